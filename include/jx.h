@@ -1,0 +1,155 @@
+/*
+ * jx -- GB300-native Jaccard engine: C ABI.
+ *
+ * Plain C, plain pointers and sizes.  Every pointer argument documented as "device" must be
+ * device (or managed) memory of the current CUDA device; "host" pointers are host memory.
+ * All calls are asynchronous on the given stream unless documented otherwise; a NULL stream
+ * is the legacy default stream.  Calls return a status code and never exit the process.
+ *
+ * Graph model (reference: standalone_csr.hpp:44-105, GraphCSRView<int32_t,int32_t,float>):
+ *   row_ptr  int32[n + 1]  CSR offsets, row_ptr[0] = 0, non-decreasing, row_ptr[n] = e
+ *   col_idx  int32[e]      neighbours of each row, each row sorted ascending, values in [0, n)
+ * Results are per stored directed edge, in CSR order (out[k] belongs to edge k).
+ *
+ * Numerics follow the reference bit for bit:
+ *   - unweighted: J = c / (d_u + d_v - c) with the reference's float expressions
+ *     (edge-centric jaccard.cpp:741, vertex-centric jaccard.cpp:258,339,617-618);
+ *   - weighted: row sums S in the reference's 32-wide scan order (jaccard.cpp:53-137) and the
+ *     intersection weight I accumulated in the order a CPU SYCL device gives the reference's
+ *     8 i-lanes (jaccard.cpp:343, 370-396): ref positions 0,8,16,..., then 1,9,17,..., ...
+ *   - IEEE float division (no fast math).
+ */
+#ifndef JX_H
+#define JX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same object as cudaStream_t. */
+typedef struct CUstream_st *jx_stream_t;
+
+typedef enum {
+  JX_OK = 0,
+  JX_ERR_INVALID = 1,     /* bad argument (NULL pointer, negative size, ...) */
+  JX_ERR_CUDA = 2,        /* a CUDA call failed; jx_last_cuda_error() has the code */
+  JX_ERR_NOMEM = 3,       /* device or host allocation failed */
+  JX_ERR_BAD_GRAPH = 4,   /* jx_csr_check found an invalid CSR */
+  JX_ERR_UNSUPPORTED = 5, /* valid request outside what this build supports */
+  JX_ERR_TOO_LARGE = 6    /* size above a documented maximum */
+} jx_status;
+
+typedef enum {
+  JX_ALGO_VERTEX_CENTRIC = 0, /* sygraph::jaccard<false, ...>  RowSum -> IS -> JW */
+  JX_ALGO_EDGE_CENTRIC = 1    /* sygraph::jaccard<true, ...>   ec_scan -> ec_unweighted */
+} jx_algo;
+
+/* Device-pointer view of an int32 CSR graph (GraphCSRView, standalone_csr.hpp:44-105). */
+typedef struct {
+  int32_t n;              /* number_of_vertices */
+  int32_t e;              /* number_of_edges (stored directed edges) */
+  const int32_t *row_ptr; /* offsets, device, n + 1 */
+  const int32_t *col_idx; /* indices, device, e */
+} jx_csr;
+
+/* Bits reported by jx_csr_check. */
+#define JX_CSR_OFFSETS_BAD 0x1u /* row_ptr[0] != 0, decreasing, or row_ptr[n] != e */
+#define JX_CSR_INDEX_RANGE 0x2u /* some col_idx outside [0, n) */
+#define JX_CSR_UNSORTED 0x4u    /* some row not sorted ascending */
+#define JX_CSR_DUPLICATE 0x8u   /* some row holds the same neighbour twice */
+#define JX_CSR_SELF_LOOP 0x10u  /* some row lists itself */
+#define JX_CSR_ASYMMETRIC 0x20u /* some edge (u,v) has no (v,u) */
+
+const char *jx_status_string(jx_status s);
+int jx_version(void);        /* 10000 * major + 100 * minor + patch */
+int jx_last_cuda_error(void); /* cudaError_t of the last JX_ERR_CUDA on this thread */
+
+/* ------------------------------------------------------------------ whole-operator calls */
+
+/*
+ * Jaccard for every stored edge: the drop-in for
+ *   sygraph::jaccard<edge_centric, int32_t, int32_t, float>(graph, [weights,] result, q)
+ * (standalone_algorithms.hpp:67-69 weighted, :86-87 unweighted; jaccard.cpp:926-955).
+ *
+ *   vertex_w  device float[n] per-vertex weights, or NULL for unweighted.  The edge-centric
+ *             algorithm ignores weights, as the reference does (jaccard.cpp:790).
+ *   out_j     device float[e], written once per edge.
+ * Temporaries are taken from the stream-ordered allocator and released before return
+ * (stream-ordered); use jx_jaccard_ws to supply them instead.  Asynchronous.
+ */
+jx_status jx_jaccard(const jx_csr *g, const float *vertex_w, float *out_j, jx_algo algo,
+                     jx_stream_t stream);
+
+/* Bytes of device workspace jx_jaccard_ws needs for this graph (a host-side bound). */
+size_t jx_jaccard_workspace_size(const jx_csr *g, int weighted, jx_algo algo);
+
+/* jx_jaccard with caller-provided device workspace (256-byte aligned, >= the size above). */
+jx_status jx_jaccard_ws(const jx_csr *g, const float *vertex_w, float *out_j, jx_algo algo,
+                        void *workspace, size_t workspace_bytes, jx_stream_t stream);
+
+/*
+ * Host-buffer form of jx_jaccard: the reference's buffers wrap host memory
+ * (main.cpp:196-200), so this entry point takes host arrays, copies them to the device,
+ * runs the operator and copies the results back.  Synchronous.  Pinned host memory gives
+ * the fastest copies; pageable memory works.
+ */
+jx_status jx_jaccard_host(int32_t n, int32_t e, const int32_t *row_ptr, const int32_t *col_idx,
+                          const float *vertex_w, float *out_j, jx_algo algo);
+
+/* ------------------------------------------------------------------ stage-level calls
+ * One call per reference kernel (the static invoke functions of jaccard.hpp), for stage
+ * parity and for callers that, like main.cpp:255-257, drive the kernels themselves.
+ */
+
+/* Jaccard_RowSumKernel<w>::invoke (jaccard.hpp:104-107, jaccard.cpp:263-313).
+ * work[r] = (float)(row_ptr[r+1]-row_ptr[r]) when w == NULL, else the reference-order sum of
+ * w[ind[k]] over the row.  `ind` is any int32[e] index array (main.cpp:213-257 passes
+ * 0..e-1 with edge weights to build vertex weights).  device pointers. */
+jx_status jx_rowsum(int32_t n, int32_t e, const int32_t *row_ptr, const int32_t *ind,
+                    const float *w, float *work, jx_stream_t stream);
+
+/* FillKernel<float>::invoke (jaccard.hpp:51-52, jaccard.cpp:161-182): x[0..n) = value. */
+jx_status jx_fill(int64_t n, float *x, float value, jx_stream_t stream);
+
+/* Jaccard_IsKernel<w>::invoke (jaccard.hpp:151-156, jaccard.cpp:402-458):
+ *   weight_s[j]  = work[row] + work[col]
+ *   weight_i[j] += sum over common neighbours (1 or w[k]), starting from weight_i[j]'s
+ *                  current value, in the reference's order.
+ * w may be NULL (unweighted).  device pointers. */
+jx_status jx_intersect(int32_t n, int32_t e, const int32_t *row_ptr, const int32_t *col_idx,
+                       const float *w, const float *work, float *weight_i, float *weight_s,
+                       jx_stream_t stream);
+
+/* Jaccard_JwKernel::invoke (jaccard.hpp:235-237, jaccard.cpp:622-653):
+ * weight_j[j] = weight_i[j] / (weight_s[j] - weight_i[j]). */
+jx_status jx_weight(int32_t e, const float *weight_i, const float *weight_s, float *weight_j,
+                    jx_stream_t stream);
+
+/* Jaccard_ec_scan::invoke (jaccard.hpp:256-258, jaccard.cpp:666-700):
+ * dest_ind[k] = row of edge k, weight_j[k] = 0. */
+jx_status jx_ec_scan(int32_t e, int32_t n, const int32_t *row_ptr, int32_t *dest_ind,
+                     float *weight_j, jx_stream_t stream);
+
+/* Jaccard_ec_unweighted::invoke (jaccard.hpp:280-283, jaccard.cpp:745-782):
+ * weight_j[k] += matches, then weight_j[k] = c / ((float)(Ni + Nj) - c). */
+jx_status jx_ec_unweighted(int32_t e, int32_t n, const int32_t *row_ptr, const int32_t *col_idx,
+                           const int32_t *dest_ind, float *weight_j, jx_stream_t stream);
+
+/* ------------------------------------------------------------------ utilities */
+
+/* Validate a CSR on the device; *flags receives JX_CSR_* bits (0 = valid, sorted, symmetric).
+ * Synchronous on `stream`. */
+jx_status jx_csr_check(const jx_csr *g, uint32_t *flags, jx_stream_t stream);
+
+/* Number of kernels this library launched on this thread since the last reset. */
+uint64_t jx_launch_count(void);
+void jx_launch_count_reset(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JX_H */

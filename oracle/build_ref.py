@@ -1,0 +1,100 @@
+"""Build recipe for the oracle side -- TEST INFRASTRUCTURE ONLY.
+
+Builds two host libraries with gcc/g++ (no GPU, no cmake):
+
+* ``oracle/libjxoracle.so`` -- the plain-C restatement of the reference algorithm
+  (``oracle/jx_oracle.c``).
+* ``oracle/_ref/libjxref.so`` -- the reference's own ``jaccard.cpp`` compiled unmodified
+  against the host SYCL subset in ``oracle/syclshim`` (``oracle/ref_driver.cpp`` includes it).
+
+The reference sources are read where they lie (``/root/reference``) or, on a machine without
+that directory, from the git-ignored copy in ``baseline/_ref/src`` that ``--install`` makes.
+Only the four files the hot path needs are used: jaccard.cpp, jaccard.hpp,
+standalone_algorithms.hpp, standalone_csr.hpp.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+REF_DIRS = ["/root/reference", os.path.join(ROOT, "baseline", "_ref", "src")]
+REF_FILES = ["jaccard.cpp", "jaccard.hpp", "standalone_algorithms.hpp", "standalone_csr.hpp"]
+ORACLE_SO = os.path.join(HERE, "libjxoracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libjxref.so")
+# The reference's shipped configuration (Makefile:33, Makefile:387, ICX flags Makefile:74).
+REF_DEFINES = ["-DSTANDALONE", "-DSYCL_1_2_1", "-DDISABLE_DP_WEIGHT", "-DDISABLE_LIST",
+               "-DDISABLE_DP_INDEX"]
+
+
+def ref_source_dir() -> str | None:
+    for d in REF_DIRS:
+        if all(os.path.isfile(os.path.join(d, f)) for f in REF_FILES):
+            return d
+    return None
+
+
+def install_copy() -> str:
+    """Copy the hot-path sources of the reference into the git-ignored baseline/_ref/src."""
+    src = REF_DIRS[0]
+    dst = REF_DIRS[1]
+    os.makedirs(dst, exist_ok=True)
+    for f in REF_FILES:
+        shutil.copy2(os.path.join(src, f), os.path.join(dst, f))
+    return dst
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+
+
+def _stale(out: str, inputs: list[str]) -> bool:
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(i) > t for i in inputs if os.path.exists(i))
+
+
+def build_oracle(force: bool = False) -> str:
+    src = os.path.join(HERE, "jx_oracle.c")
+    if force or _stale(ORACLE_SO, [src]):
+        _run(["gcc", "-O2", "-std=c11", "-fopenmp", "-fPIC", "-shared", "-o", ORACLE_SO, src, "-lm"])
+    return ORACLE_SO
+
+
+def build_ref(force: bool = False) -> str | None:
+    d = ref_source_dir()
+    if d is None:
+        return None
+    os.makedirs(os.path.dirname(REF_SO), exist_ok=True)
+    srcs = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "syclshim", "syclshim.cpp")]
+    deps = srcs + [os.path.join(HERE, "syclshim", "CL", "sycl.hpp")] + [os.path.join(d, f) for f in REF_FILES]
+    if force or _stale(REF_SO, deps):
+        _run(["g++", "-O3", "-std=c++20", "-fopenmp", "-fPIC", "-shared", "-w",
+              "-U_FORTIFY_SOURCE", "-D_FORTIFY_SOURCE=0",
+              "-I", os.path.join(HERE, "syclshim"), "-I", d, *REF_DEFINES,
+              "-o", REF_SO, *srcs])
+    return REF_SO
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--install", action="store_true",
+                    help="copy the reference's hot-path sources into baseline/_ref/src")
+    ap.add_argument("--force", action="store_true")
+    a = ap.parse_args()
+    if a.install:
+        print("copied reference sources to", install_copy())
+    print("oracle:", build_oracle(a.force))
+    print("reference:", build_ref(a.force) or "unavailable (no reference sources)")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

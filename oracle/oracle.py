@@ -1,0 +1,188 @@
+"""ctypes bindings for the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only the tests, the smoke check of ``__graft_entry__`` and the CPU-baseline leg of
+``bench.py`` import this module.  It wraps:
+
+* ``libjxoracle.so``: the C restatement of the reference algorithm (``jx_oracle.c``);
+* ``_ref/libjxref.so``: the reference's own ``jaccard.cpp`` run through the host SYCL
+  subset (``ref_driver.cpp``), when it could be built.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build_ref
+
+_I32 = ctypes.POINTER(ctypes.c_int32)
+_F32 = ctypes.POINTER(ctypes.c_float)
+_F64 = ctypes.POINTER(ctypes.c_double)
+
+_oracle = None
+_ref = None
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+def lib():
+    global _oracle
+    if _oracle is None:
+        build_ref.build_oracle()
+        L = ctypes.CDLL(build_ref.ORACLE_SO)
+        L.jxo_rowsum.argtypes = [ctypes.c_int32, _I32, _I32, _F32, _F32, ctypes.c_int]
+        L.jxo_intersect_rows.argtypes = [ctypes.c_int32, ctypes.c_int32, _I32, _I32, _F32, _F32,
+                                         _F32, _F32, ctypes.c_int]
+        L.jxo_weight.argtypes = [ctypes.c_int64, _F32, _F32, _F32]
+        L.jxo_ec_scan.argtypes = [ctypes.c_int32, _I32, _I32, _F32]
+        L.jxo_ec_edges.argtypes = [ctypes.c_int64, ctypes.c_int64, _I32, _I32, _I32, _F32,
+                                   ctypes.c_int]
+        L.jxo_jaccard_rows.argtypes = [ctypes.c_int, ctypes.c_int32, _I32, _I32, _F32,
+                                       ctypes.c_int32, ctypes.c_int32, _F32, _F32, ctypes.c_int]
+        L.jxo_jaccard_rows.restype = ctypes.c_int
+        L.jxo_counts_rows.argtypes = [ctypes.c_int32, ctypes.c_int32, _I32, _I32, _I32,
+                                      ctypes.c_int]
+        L.jxo_jaccard_f64_rows.argtypes = [ctypes.c_int32, _I32, _I32, _F32, ctypes.c_int32,
+                                           ctypes.c_int32, _F64, ctypes.c_int]
+        _oracle = L
+    return _oracle
+
+
+def ref_lib():
+    """The reference via the SYCL subset, or None when its sources are not available."""
+    global _ref
+    if _ref is None:
+        so = build_ref.build_ref()
+        if so is None:
+            if os.path.exists(build_ref.REF_SO):
+                so = build_ref.REF_SO
+            else:
+                return None
+        L = ctypes.CDLL(so)
+        L.jxref_set_threads.argtypes = [ctypes.c_int]
+        L.jxref_set_group_sample.argtypes = [ctypes.c_int]
+        L.jxref_jaccard.argtypes = [ctypes.c_int, ctypes.c_int32, ctypes.c_int32, _I32, _I32, _F32,
+                                    _F32]
+        L.jxref_rowsum.argtypes = [ctypes.c_int32, ctypes.c_int32, _I32, _I32, _F32, _F32]
+        L.jxref_fill.argtypes = [ctypes.c_int64, _F32, ctypes.c_float]
+        L.jxref_intersect.argtypes = [ctypes.c_int32, ctypes.c_int32, _I32, _I32, _F32, _F32, _F32,
+                                      _F32]
+        L.jxref_weight.argtypes = [ctypes.c_int32, _F32, _F32, _F32]
+        L.jxref_ec_scan.argtypes = [ctypes.c_int32, ctypes.c_int32, _I32, _I32, _F32]
+        L.jxref_ec_unweighted.argtypes = [ctypes.c_int32, ctypes.c_int32, _I32, _I32, _I32, _F32]
+        _ref = L
+    return _ref
+
+
+# ---------------------------------------------------------------- C restatement wrappers
+
+def rowsum(row_ptr, ind, w=None, threads=0):
+    n = len(row_ptr) - 1
+    out = np.empty(n, np.float32)
+    lib().jxo_rowsum(n, _p(row_ptr, _I32), _p(ind, _I32), _p(w, _F32), _p(out, _F32), threads)
+    return out
+
+
+def intersect(row_ptr, col, w, work, weight_i, threads=0):
+    """Jaccard_IsKernel over all rows; weight_i (float32[E]) accumulates in place."""
+    n = len(row_ptr) - 1
+    ws = np.empty(len(col), np.float32)
+    lib().jxo_intersect_rows(0, n, _p(row_ptr, _I32), _p(col, _I32), _p(w, _F32), _p(work, _F32),
+                             _p(weight_i, _F32), _p(ws, _F32), threads)
+    return ws
+
+
+def weight(weight_i, weight_s):
+    out = np.empty(len(weight_i), np.float32)
+    lib().jxo_weight(len(weight_i), _p(weight_i, _F32), _p(weight_s, _F32), _p(out, _F32))
+    return out
+
+
+def jaccard(row_ptr, col, w=None, edge_centric=False, rows=None, threads=0):
+    """sygraph::jaccard restated; `rows=(r0, r1)` limits the output to those rows' edges."""
+    n = len(row_ptr) - 1
+    r0, r1 = rows if rows is not None else (0, n)
+    out = np.empty(int(row_ptr[r1]) - int(row_ptr[r0]), np.float32)
+    rc = lib().jxo_jaccard_rows(1 if edge_centric else 0, n, _p(row_ptr, _I32), _p(col, _I32),
+                                _p(w, _F32), r0, r1, None, _p(out, _F32), threads)
+    if rc != 0:
+        raise MemoryError("oracle allocation failed")
+    return out
+
+
+def counts(row_ptr, col, rows=None, threads=0):
+    n = len(row_ptr) - 1
+    r0, r1 = rows if rows is not None else (0, n)
+    out = np.empty(int(row_ptr[r1]) - int(row_ptr[r0]), np.int32)
+    lib().jxo_counts_rows(r0, r1, _p(row_ptr, _I32), _p(col, _I32), _p(out, _I32), threads)
+    return out
+
+
+def jaccard_f64(row_ptr, col, w=None, rows=None, threads=0):
+    n = len(row_ptr) - 1
+    r0, r1 = rows if rows is not None else (0, n)
+    out = np.empty(int(row_ptr[r1]) - int(row_ptr[r0]), np.float64)
+    lib().jxo_jaccard_f64_rows(n, _p(row_ptr, _I32), _p(col, _I32), _p(w, _F32), r0, r1,
+                               _p(out, _F64), threads)
+    return out
+
+
+# ---------------------------------------------------------------- reference (via SYCL subset)
+
+def ref_jaccard(row_ptr, col, w=None, edge_centric=False, threads=0, group_sample=1):
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("reference sources unavailable")
+    L.jxref_set_threads(threads)
+    L.jxref_set_group_sample(group_sample)
+    n = len(row_ptr) - 1
+    out = np.zeros(len(col), np.float32)
+    try:
+        L.jxref_jaccard(1 if edge_centric else 0, n, len(col), _p(row_ptr, _I32), _p(col, _I32),
+                        _p(w, _F32), _p(out, _F32))
+    finally:
+        L.jxref_set_group_sample(1)
+    return out
+
+
+def ref_rowsum(row_ptr, ind, w=None, threads=0):
+    L = ref_lib()
+    L.jxref_set_threads(threads)
+    n = len(row_ptr) - 1
+    out = np.empty(n, np.float32)
+    L.jxref_rowsum(n, len(ind), _p(row_ptr, _I32), _p(ind, _I32), _p(w, _F32), _p(out, _F32))
+    return out
+
+
+def ref_intersect(row_ptr, col, w, work, weight_i, threads=0):
+    L = ref_lib()
+    L.jxref_set_threads(threads)
+    n = len(row_ptr) - 1
+    ws = np.empty(len(col), np.float32)
+    L.jxref_intersect(n, len(col), _p(row_ptr, _I32), _p(col, _I32), _p(w, _F32), _p(work, _F32),
+                      _p(weight_i, _F32), _p(ws, _F32))
+    return ws
+
+
+def ref_weight(weight_i, weight_s):
+    out = np.empty(len(weight_i), np.float32)
+    ref_lib().jxref_weight(len(weight_i), _p(weight_i, _F32), _p(weight_s, _F32), _p(out, _F32))
+    return out
+
+
+def ref_ec_scan(row_ptr, e):
+    n = len(row_ptr) - 1
+    dest = np.empty(e, np.int32)
+    wj = np.full(e, np.nan, np.float32)
+    ref_lib().jxref_ec_scan(e, n, _p(row_ptr, _I32), _p(dest, _I32), _p(wj, _F32))
+    return dest, wj
+
+
+def ref_ec_unweighted(row_ptr, col, dest, weight_j):
+    n = len(row_ptr) - 1
+    ref_lib().jxref_ec_unweighted(len(col), n, _p(row_ptr, _I32), _p(col, _I32), _p(dest, _I32),
+                                  _p(weight_j, _F32))
+    return weight_j

@@ -1,0 +1,153 @@
+/*
+ * C entry points around the reference's own Jaccard code -- TEST INFRASTRUCTURE ONLY.
+ *
+ * This translation unit includes the reference's `jaccard.cpp` (vtsynergy/SYCL-Jaccard)
+ * unmodified, compiled against the host SYCL subset in oracle/syclshim with the reference's
+ * shipped flags (Makefile:33: -DDISABLE_DP_WEIGHT -DDISABLE_LIST -DDISABLE_DP_INDEX, plus
+ * -DSTANDALONE -DSYCL_1_2_1 as its Makefile:387 and ICX flags give).  The source directory
+ * is put on the include path by oracle/build_ref.py; no reference source lives in this
+ * repository.
+ *
+ * Entry points mirror the reference's public and kernel-level calls:
+ *   jxref_jaccard        sygraph::jaccard<edge_centric>(graph, [weights,] result, q)
+ *                        (standalone_algorithms.hpp:67-87, jaccard.cpp:926-955)
+ *   jxref_rowsum         detail::Jaccard_RowSumKernel<w>::invoke   (jaccard.cpp:263-313)
+ *   jxref_fill           FillKernel<float>::invoke                  (jaccard.cpp:161-182)
+ *   jxref_intersect      detail::Jaccard_IsKernel<w>::invoke       (jaccard.cpp:402-458)
+ *   jxref_weight         detail::Jaccard_JwKernel::invoke           (jaccard.cpp:622-653)
+ *   jxref_ec_scan        detail::Jaccard_ec_scan::invoke            (jaccard.cpp:666-700)
+ *   jxref_ec_unweighted  detail::Jaccard_ec_unweighted::invoke      (jaccard.cpp:745-782)
+ * The edge-centric driver prints a line to std::cout (jaccard.cpp:819); it is discarded.
+ */
+#include "jaccard.cpp"
+
+#include <cstdint>
+#include <iostream>
+#include <streambuf>
+
+namespace {
+struct NullBuf : std::streambuf {
+  int overflow(int c) override { return c; }
+};
+
+struct MuteCout {
+  NullBuf nb;
+  std::streambuf *old;
+  MuteCout() : old(std::cout.rdbuf(&nb)) {}
+  ~MuteCout() { std::cout.rdbuf(old); }
+};
+
+template <typename T> cl::sycl::buffer<T> wrap(const T *p, int64_t n) {
+  return cl::sycl::buffer<T>(const_cast<T *>(p), cl::sycl::range<1>((size_t)n));
+}
+} // namespace
+
+extern "C" {
+
+void jxref_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+
+/* Execute only every k-th work-group of each launch (timing samples); 1 = everything. */
+void jxref_set_group_sample(int k) { jxshim::set_group_sample(k); }
+
+int jxref_jaccard(int edge_centric, int32_t n, int32_t e, const int32_t *row_ptr,
+                  const int32_t *col, const float *vertex_w, float *out) {
+  MuteCout mute;
+  cl::sycl::queue q;
+  GraphCSRView<int32_t, int32_t, float> g(wrap(row_ptr, (int64_t)n + 1), wrap(col, e),
+                                          cl::sycl::buffer<float>(nullptr), n, e);
+  cl::sycl::buffer<float> result(out, cl::sycl::range<1>((size_t)e));
+  if (vertex_w) {
+    cl::sycl::buffer<float> wb = wrap(vertex_w, n);
+    if (edge_centric)
+      sygraph::jaccard<true, int32_t, int32_t, float>(g, wb, result, q);
+    else
+      sygraph::jaccard<false, int32_t, int32_t, float>(g, wb, result, q);
+  } else {
+    if (edge_centric)
+      sygraph::jaccard<true, int32_t, int32_t, float>(g, result, q);
+    else
+      sygraph::jaccard<false, int32_t, int32_t, float>(g, result, q);
+  }
+  return 0;
+}
+
+int jxref_rowsum(int32_t n, int32_t e, const int32_t *row_ptr, const int32_t *ind,
+                 const float *w, float *work) {
+  cl::sycl::queue q;
+  auto rp = wrap(row_ptr, (int64_t)n + 1);
+  auto ci = wrap(ind, e);
+  cl::sycl::buffer<float> wk(work, cl::sycl::range<1>((size_t)n));
+  if (w) {
+    auto wb = wrap(w, e); /* the vertex-weight array must cover every index in `ind` */
+    sygraph::detail::Jaccard_RowSumKernel<true, int32_t, int32_t, float>::invoke(n, e, rp, ci, &wb,
+                                                                                wk, q);
+  } else {
+    sygraph::detail::Jaccard_RowSumKernel<false, int32_t, int32_t, float>::invoke(n, e, rp, ci,
+                                                                                 nullptr, wk, q);
+  }
+  return 0;
+}
+
+int jxref_fill(int64_t n, float *x, float value) {
+  cl::sycl::queue q;
+  cl::sycl::buffer<float> xb(x, cl::sycl::range<1>((size_t)n));
+  FillKernel<float>::invoke((size_t)n, xb, value, q);
+  return 0;
+}
+
+int jxref_intersect(int32_t n, int32_t e, const int32_t *row_ptr, const int32_t *col,
+                    const float *w, const float *work, float *weight_i, float *weight_s) {
+  cl::sycl::queue q;
+  auto rp = wrap(row_ptr, (int64_t)n + 1);
+  auto ci = wrap(col, e);
+  auto wk = wrap(work, n);
+  cl::sycl::buffer<float> wi(weight_i, cl::sycl::range<1>((size_t)e));
+  cl::sycl::buffer<float> ws(weight_s, cl::sycl::range<1>((size_t)e));
+  if (w) {
+    auto wb = wrap(w, n);
+    sygraph::detail::Jaccard_IsKernel<true, int32_t, int32_t, float>::invoke(n, e, rp, ci, &wb, wk,
+                                                                            wi, ws, q);
+  } else {
+    sygraph::detail::Jaccard_IsKernel<false, int32_t, int32_t, float>::invoke(n, e, rp, ci, nullptr,
+                                                                             wk, wi, ws, q);
+  }
+  return 0;
+}
+
+int jxref_weight(int32_t e, const float *weight_i, const float *weight_s, float *weight_j) {
+  cl::sycl::queue q;
+  auto wi = wrap(weight_i, e);
+  auto ws = wrap(weight_s, e);
+  cl::sycl::buffer<float> wj(weight_j, cl::sycl::range<1>((size_t)e));
+  sygraph::detail::Jaccard_JwKernel<int32_t, int32_t, float>::invoke(e, wi, ws, wj, q);
+  return 0;
+}
+
+int jxref_ec_scan(int32_t e, int32_t n, const int32_t *row_ptr, int32_t *dest_ind,
+                  float *weight_j) {
+  cl::sycl::queue q;
+  auto rp = wrap(row_ptr, (int64_t)n + 1);
+  cl::sycl::buffer<int32_t> di(dest_ind, cl::sycl::range<1>((size_t)e));
+  cl::sycl::buffer<float> wj(weight_j, cl::sycl::range<1>((size_t)e));
+  sygraph::detail::Jaccard_ec_scan<int32_t, int32_t, float>::invoke(e, n, rp, di, wj, q);
+  return 0;
+}
+
+int jxref_ec_unweighted(int32_t e, int32_t n, const int32_t *row_ptr, const int32_t *col,
+                        const int32_t *dest_ind, float *weight_j) {
+  cl::sycl::queue q;
+  auto rp = wrap(row_ptr, (int64_t)n + 1);
+  auto ci = wrap(col, e);
+  auto di = wrap(dest_ind, e);
+  cl::sycl::buffer<float> wj(weight_j, cl::sycl::range<1>((size_t)e));
+  sygraph::detail::Jaccard_ec_unweighted<int32_t, int32_t, float>::invoke(e, n, rp, ci, di, wj, q);
+  return 0;
+}
+
+} /* extern "C" */

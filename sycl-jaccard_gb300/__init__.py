@@ -1,0 +1,279 @@
+"""jx: GB300-native Jaccard engine -- Python host mirror of the reference operator surface.
+
+The compute path is ``csrc/libjx.so`` (hand-written sm_103a CUDA kernels behind a C ABI,
+``include/jx.h``).  This module binds it with ctypes and mirrors the reference's API
+(vtsynergy/SYCL-Jaccard, ``standalone_algorithms.hpp:67-87``, ``jaccard.hpp``):
+
+* :class:`GraphCSRView` -- ``standalone_csr.hpp:44-105`` over device tensors;
+* :func:`jaccard` -- ``sygraph::jaccard<edge_centric>(graph, [weights,] result, q)``;
+* :func:`rowsum`, :func:`fill`, :func:`intersect`, :func:`weight`, :func:`ec_scan`,
+  :func:`ec_unweighted` -- the kernel-level ``invoke`` statics of ``jaccard.hpp``;
+* :func:`jaccard_host` -- the same operator on host (numpy) arrays, like the reference's
+  buffers that wrap host memory.
+
+PyTorch supplies device memory and streams only.  There is no CPU fallback: if the native
+library is missing or no GPU is present, calls raise.
+
+The package directory name contains a hyphen, so import it with
+``importlib.import_module("sycl-jaccard_gb300")``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+from . import graphgen  # noqa: F401  (synthetic graphs)
+
+__all__ = ["GraphCSRView", "JxError", "jaccard", "jaccard_host", "rowsum", "fill", "intersect",
+           "weight", "ec_scan", "ec_unweighted", "csr_check", "lib", "launch_count",
+           "launch_count_reset", "graphgen"]
+
+JX_OK = 0
+_STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory",
+           4: "invalid CSR graph", 5: "unsupported request", 6: "size above the supported maximum"}
+ALGO_VERTEX_CENTRIC = 0
+ALGO_EDGE_CENTRIC = 1
+
+CSR_FLAGS = {0x1: "offsets_bad", 0x2: "index_range", 0x4: "unsorted", 0x8: "duplicate",
+             0x10: "self_loop", 0x20: "asymmetric"}
+
+
+class JxError(RuntimeError):
+    def __init__(self, status: int, what: str):
+        self.status = status
+        msg = f"{what}: {_STATUS.get(status, 'unknown status')} ({status})"
+        if status == 2 and _lib is not None:
+            msg += f", cudaError {_lib.jx_last_cuda_error()}"
+        super().__init__(msg)
+
+
+class _Csr(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("e", ctypes.c_int32), ("row_ptr", ctypes.c_void_p),
+                ("col_idx", ctypes.c_void_p)]
+
+
+_lib = None
+_VP = ctypes.c_void_p
+
+
+def lib() -> ctypes.CDLL:
+    """Load libjx.so (building it first if sources are newer); raise if it cannot load."""
+    global _lib
+    if _lib is None:
+        so = _build.LIBJX
+        if not os.path.exists(so):
+            try:
+                _build.build_engine()
+            except Exception as exc:  # pragma: no cover - depends on the machine
+                raise RuntimeError(f"jx native library missing and could not be built: {exc}") from exc
+        L = ctypes.CDLL(so)
+        i32, i64, f32, u32p = ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.POINTER(ctypes.c_uint32)
+        sig = {
+            "jx_jaccard": ([ctypes.POINTER(_Csr), _VP, _VP, ctypes.c_int, _VP], ctypes.c_int),
+            "jx_jaccard_ws": ([ctypes.POINTER(_Csr), _VP, _VP, ctypes.c_int, _VP, ctypes.c_size_t, _VP], ctypes.c_int),
+            "jx_jaccard_workspace_size": ([ctypes.POINTER(_Csr), ctypes.c_int, ctypes.c_int], ctypes.c_size_t),
+            "jx_jaccard_host": ([i32, i32, _VP, _VP, _VP, _VP, ctypes.c_int], ctypes.c_int),
+            "jx_rowsum": ([i32, i32, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
+            "jx_fill": ([i64, _VP, f32, _VP], ctypes.c_int),
+            "jx_intersect": ([i32, i32, _VP, _VP, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
+            "jx_weight": ([i32, _VP, _VP, _VP, _VP], ctypes.c_int),
+            "jx_ec_scan": ([i32, i32, _VP, _VP, _VP, _VP], ctypes.c_int),
+            "jx_ec_unweighted": ([i32, i32, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
+            "jx_csr_check": ([ctypes.POINTER(_Csr), u32p, _VP], ctypes.c_int),
+            "jx_status_string": ([ctypes.c_int], ctypes.c_char_p),
+            "jx_version": ([], ctypes.c_int),
+            "jx_last_cuda_error": ([], ctypes.c_int),
+            "jx_launch_count": ([], ctypes.c_uint64),
+            "jx_launch_count_reset": ([], None),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def _check(status: int, what: str) -> None:
+    if status != JX_OK:
+        raise JxError(status, what)
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("jx needs a CUDA GPU: torch.cuda.is_available() is False")
+    return torch
+
+
+def _stream(stream):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def _ptr(t, dtype, n, what):
+    if t is None:
+        return None
+    torch = _torch()
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError(f"{what} must be a CUDA tensor")
+    if t.dtype != dtype or not t.is_contiguous() or t.numel() < n:
+        raise TypeError(f"{what} must be a contiguous {dtype} tensor with at least {n} elements")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class GraphCSRView:
+    """Non-owning CSR view over device tensors (``standalone_csr.hpp:44-105``).
+
+    ``offsets``: int32[V+1] (device), ``indices``: int32[E] (device), each row sorted
+    ascending; ``edge_data`` is kept for surface parity and unused by Jaccard.
+    """
+
+    def __init__(self, offsets, indices, edge_data=None, number_of_vertices=None,
+                 number_of_edges=None):
+        torch = _torch()
+        self.offsets = offsets
+        self.indices = indices
+        self.edge_data = edge_data
+        self.number_of_vertices = int(number_of_vertices if number_of_vertices is not None
+                                      else offsets.numel() - 1)
+        self.number_of_edges = int(number_of_edges if number_of_edges is not None
+                                   else indices.numel())
+        _ptr(offsets, torch.int32, self.number_of_vertices + 1, "offsets")
+        _ptr(indices, torch.int32, self.number_of_edges, "indices")
+
+    @classmethod
+    def from_numpy(cls, row_ptr: np.ndarray, col_idx: np.ndarray, device="cuda"):
+        torch = _torch()
+        return cls(torch.from_numpy(np.ascontiguousarray(row_ptr, np.int32)).to(device),
+                   torch.from_numpy(np.ascontiguousarray(col_idx, np.int32)).to(device))
+
+    def _c(self) -> _Csr:
+        return _Csr(self.number_of_vertices, self.number_of_edges, self.offsets.data_ptr(),
+                    self.indices.data_ptr())
+
+
+def jaccard(graph: GraphCSRView, weights=None, result=None, edge_centric: bool = False,
+            stream=None, workspace=None):
+    """``sygraph::jaccard<edge_centric>(graph, [weights,] result, q)``.
+
+    ``weights``: float32[V] device tensor of per-vertex weights, or None (unweighted).  The
+    edge-centric algorithm ignores weights, as the reference does.  ``result``: float32[E]
+    device tensor (allocated when None).  Asynchronous on ``stream``.  Returns ``result``.
+    """
+    torch = _torch()
+    E = graph.number_of_edges
+    if result is None:
+        result = torch.empty(E, dtype=torch.float32, device=graph.indices.device)
+    wp = _ptr(weights, torch.float32, graph.number_of_vertices, "weights")
+    rp = _ptr(result, torch.float32, E, "result")
+    algo = ALGO_EDGE_CENTRIC if edge_centric else ALGO_VERTEX_CENTRIC
+    g = graph._c()
+    L = lib()
+    if workspace is None:
+        _check(L.jx_jaccard(ctypes.byref(g), wp, rp, algo, _stream(stream)), "jx_jaccard")
+    else:
+        _check(L.jx_jaccard_ws(ctypes.byref(g), wp, rp, algo, ctypes.c_void_p(workspace.data_ptr()),
+                               workspace.numel() * workspace.element_size(), _stream(stream)),
+               "jx_jaccard_ws")
+    return result
+
+
+def workspace_size(graph: GraphCSRView, weighted: bool, edge_centric: bool = False) -> int:
+    g = graph._c()
+    return int(lib().jx_jaccard_workspace_size(ctypes.byref(g), int(weighted),
+                                                ALGO_EDGE_CENTRIC if edge_centric else ALGO_VERTEX_CENTRIC))
+
+
+def jaccard_host(row_ptr: np.ndarray, col_idx: np.ndarray, weights: np.ndarray | None = None,
+                 edge_centric: bool = False, out: np.ndarray | None = None) -> np.ndarray:
+    """Host-array form: copies in, computes on the GPU, copies out (synchronous)."""
+    row_ptr = np.ascontiguousarray(row_ptr, np.int32)
+    col_idx = np.ascontiguousarray(col_idx, np.int32)
+    n, e = len(row_ptr) - 1, len(col_idx)
+    if out is None:
+        out = np.empty(e, np.float32)
+    w = None if weights is None else np.ascontiguousarray(weights, np.float32)
+    algo = ALGO_EDGE_CENTRIC if edge_centric else ALGO_VERTEX_CENTRIC
+    _check(lib().jx_jaccard_host(n, e, row_ptr.ctypes.data, col_idx.ctypes.data,
+                                 None if w is None else w.ctypes.data, out.ctypes.data, algo),
+           "jx_jaccard_host")
+    return out
+
+
+# ------------------------------------------------------------------ stage-level surface
+
+def rowsum(n, e, offsets, indices, weights, work, stream=None):
+    """``Jaccard_RowSumKernel<weighted>::invoke`` (jaccard.cpp:263-313)."""
+    torch = _torch()
+    _check(lib().jx_rowsum(n, e, _ptr(offsets, torch.int32, n + 1, "offsets"),
+                           _ptr(indices, torch.int32, e, "indices") if e > 0 else None,
+                           _ptr(weights, torch.float32, 1, "weights"),
+                           _ptr(work, torch.float32, n, "work"), _stream(stream)), "jx_rowsum")
+    return work
+
+
+def fill(x, value: float, n=None, stream=None):
+    """``FillKernel<float>::invoke`` (jaccard.cpp:161-182)."""
+    torch = _torch()
+    n = x.numel() if n is None else n
+    _check(lib().jx_fill(n, _ptr(x, torch.float32, n, "x"), float(value), _stream(stream)), "jx_fill")
+    return x
+
+
+def intersect(n, e, offsets, indices, weights, work, weight_i, weight_s, stream=None):
+    """``Jaccard_IsKernel<weighted>::invoke`` (jaccard.cpp:402-458); weight_i accumulates."""
+    torch = _torch()
+    _check(lib().jx_intersect(n, e, _ptr(offsets, torch.int32, n + 1, "offsets"),
+                              _ptr(indices, torch.int32, e, "indices"),
+                              _ptr(weights, torch.float32, n, "weights"),
+                              _ptr(work, torch.float32, n, "work"),
+                              _ptr(weight_i, torch.float32, e, "weight_i"),
+                              _ptr(weight_s, torch.float32, e, "weight_s"), _stream(stream)),
+           "jx_intersect")
+
+
+def weight(e, weight_i, weight_s, weight_j, stream=None):
+    """``Jaccard_JwKernel::invoke`` (jaccard.cpp:622-653)."""
+    torch = _torch()
+    _check(lib().jx_weight(e, _ptr(weight_i, torch.float32, e, "weight_i"),
+                           _ptr(weight_s, torch.float32, e, "weight_s"),
+                           _ptr(weight_j, torch.float32, e, "weight_j"), _stream(stream)), "jx_weight")
+
+
+def ec_scan(e, n, offsets, dest_ind, weight_j, stream=None):
+    """``Jaccard_ec_scan::invoke`` (jaccard.cpp:666-700)."""
+    torch = _torch()
+    _check(lib().jx_ec_scan(e, n, _ptr(offsets, torch.int32, n + 1, "offsets"),
+                            _ptr(dest_ind, torch.int32, e, "dest_ind"),
+                            _ptr(weight_j, torch.float32, e, "weight_j"), _stream(stream)), "jx_ec_scan")
+
+
+def ec_unweighted(e, n, offsets, indices, dest_ind, weight_j, stream=None):
+    """``Jaccard_ec_unweighted::invoke`` (jaccard.cpp:745-782)."""
+    torch = _torch()
+    _check(lib().jx_ec_unweighted(e, n, _ptr(offsets, torch.int32, n + 1, "offsets"),
+                                  _ptr(indices, torch.int32, e, "indices"),
+                                  _ptr(dest_ind, torch.int32, e, "dest_ind"),
+                                  _ptr(weight_j, torch.float32, e, "weight_j"), _stream(stream)),
+           "jx_ec_unweighted")
+
+
+def csr_check(graph: GraphCSRView, stream=None) -> set:
+    """Validate the CSR on the device; returns the set of problems found (empty = valid)."""
+    flags = ctypes.c_uint32(0)
+    g = graph._c()
+    _check(lib().jx_csr_check(ctypes.byref(g), ctypes.byref(flags), _stream(stream)), "jx_csr_check")
+    return {name for bit, name in CSR_FLAGS.items() if flags.value & bit}
+
+
+def launch_count() -> int:
+    return int(lib().jx_launch_count())
+
+
+def launch_count_reset() -> None:
+    lib().jx_launch_count_reset()

@@ -1,0 +1,178 @@
+// C-ABI plumbing: status strings, error/launch bookkeeping, the host-buffer entry point and
+// the CSR validator.
+#include "jx_common.cuh"
+
+#include <mutex>
+#include <vector>
+
+namespace jx {
+
+static thread_local int tl_last_cuda = 0;
+static thread_local uint64_t tl_launches = 0;
+
+jx_status set_cuda_error(cudaError_t e) {
+  tl_last_cuda = (int)e;
+  return e == cudaErrorMemoryAllocation ? JX_ERR_NOMEM : JX_ERR_CUDA;
+}
+
+void count_launches(uint64_t k) { tl_launches += k; }
+
+int sm_count() {
+  static std::mutex mu;
+  static std::vector<int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
+  if (cache[dev] == 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = v > 0 ? v : 1;
+  }
+  return cache[dev];
+}
+
+// ---------------------------------------------------------------- CSR validation
+__global__ void check_rows_kernel(int32_t n, int32_t e, const int32_t *__restrict__ row_ptr,
+                                  const int32_t *__restrict__ col, uint32_t *__restrict__ flags) {
+  uint32_t f = 0;
+  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u <= n;
+       u += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t a = row_ptr[u];
+    if (u == 0 && a != 0) f |= JX_CSR_OFFSETS_BAD;
+    if (u == n) {
+      if (a != e) f |= JX_CSR_OFFSETS_BAD;
+      continue;
+    }
+    const int32_t b = row_ptr[u + 1];
+    if (b < a || a < 0 || b > e) {
+      f |= JX_CSR_OFFSETS_BAD;
+      continue;
+    }
+    int32_t prev = -1;
+    for (int32_t k = a; k < b; ++k) {
+      const int32_t c = col[k];
+      if (c < 0 || c >= n) f |= JX_CSR_INDEX_RANGE;
+      if (c == (int32_t)u) f |= JX_CSR_SELF_LOOP;
+      if (k > a) {
+        if (c < prev) f |= JX_CSR_UNSORTED;
+        if (c == prev) f |= JX_CSR_DUPLICATE;
+      }
+      prev = c;
+    }
+  }
+  if (f) atomicOr(flags, f);
+}
+
+// Requires offsets valid, indices in range and rows sorted.
+__global__ void check_symmetry_kernel(int32_t n, const int32_t *__restrict__ row_ptr,
+                                      const int32_t *__restrict__ col, uint32_t *__restrict__ flags) {
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  bool bad = false;
+  for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += nwarps) {
+    const int32_t a = row_ptr[u], b = row_ptr[u + 1];
+    for (int32_t k = a + lane; k < b; k += 32) {
+      const int32_t v = col[k];
+      if (!bsearch_found(col, row_ptr[v], row_ptr[v + 1] - 1, (int32_t)u)) bad = true;
+    }
+  }
+  if (__any_sync(kFull, bad) && lane == 0) atomicOr(flags, JX_CSR_ASYMMETRIC);
+}
+
+} // namespace jx
+
+using namespace jx;
+
+extern "C" {
+
+const char *jx_status_string(jx_status s) {
+  switch (s) {
+  case JX_OK: return "ok";
+  case JX_ERR_INVALID: return "invalid argument";
+  case JX_ERR_CUDA: return "CUDA error";
+  case JX_ERR_NOMEM: return "out of memory";
+  case JX_ERR_BAD_GRAPH: return "invalid CSR graph";
+  case JX_ERR_UNSUPPORTED: return "unsupported request";
+  case JX_ERR_TOO_LARGE: return "size above the supported maximum";
+  }
+  return "unknown status";
+}
+
+int jx_version(void) { return 10000; }
+int jx_last_cuda_error(void) { return tl_last_cuda; }
+uint64_t jx_launch_count(void) { return tl_launches; }
+void jx_launch_count_reset(void) { tl_launches = 0; }
+
+jx_status jx_csr_check(const jx_csr *g, uint32_t *flags, jx_stream_t stream) {
+  if (!g || !flags || g->n < 0 || g->e < 0) return JX_ERR_INVALID;
+  *flags = 0;
+  if (g->n == 0) return JX_OK;
+  if (!g->row_ptr || (g->e > 0 && !g->col_idx)) return JX_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  uint32_t *d = nullptr;
+  cudaError_t ce = cudaMallocAsync(&d, sizeof(uint32_t), s);
+  if (ce != cudaSuccess) return set_cuda_error(ce);
+  jx_status st = JX_OK;
+  uint32_t h = 0;
+  do {
+    if ((ce = cudaMemsetAsync(d, 0, sizeof(uint32_t), s)) != cudaSuccess) { st = set_cuda_error(ce); break; }
+    check_rows_kernel<<<sm_count() * 8, 256, 0, s>>>(g->n, g->e, g->row_ptr, g->col_idx, d);
+    if ((st = check_launch()) != JX_OK) break;
+    if ((ce = cudaMemcpyAsync(&h, d, sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess) { st = set_cuda_error(ce); break; }
+    if ((ce = cudaStreamSynchronize(s)) != cudaSuccess) { st = set_cuda_error(ce); break; }
+    if (h & (JX_CSR_OFFSETS_BAD | JX_CSR_INDEX_RANGE | JX_CSR_UNSORTED)) break; // symmetry test needs them
+    check_symmetry_kernel<<<sm_count() * 8, 256, 0, s>>>(g->n, g->row_ptr, g->col_idx, d);
+    if ((st = check_launch()) != JX_OK) break;
+    if ((ce = cudaMemcpyAsync(&h, d, sizeof(uint32_t), cudaMemcpyDeviceToHost, s)) != cudaSuccess) { st = set_cuda_error(ce); break; }
+    if ((ce = cudaStreamSynchronize(s)) != cudaSuccess) { st = set_cuda_error(ce); break; }
+  } while (0);
+  cudaFreeAsync(d, s);
+  *flags = h;
+  return st;
+}
+
+jx_status jx_jaccard_host(int32_t n, int32_t e, const int32_t *row_ptr, const int32_t *col_idx,
+                          const float *vertex_w, float *out_j, jx_algo algo) {
+  if (n < 0 || e < 0) return JX_ERR_INVALID;
+  if (n == 0 || e == 0) return JX_OK;
+  if (!row_ptr || !col_idx || !out_j) return JX_ERR_INVALID;
+  cudaStream_t s = nullptr;
+  cudaError_t ce = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) return set_cuda_error(ce);
+  const bool weighted = vertex_w && algo == JX_ALGO_VERTEX_CENTRIC;
+  int32_t *d_rp = nullptr, *d_col = nullptr;
+  float *d_w = nullptr, *d_out = nullptr;
+  jx_status st = JX_OK;
+  do {
+    if ((ce = cudaMallocAsync(&d_rp, sizeof(int32_t) * ((size_t)n + 1), s)) != cudaSuccess ||
+        (ce = cudaMallocAsync(&d_col, sizeof(int32_t) * (size_t)e, s)) != cudaSuccess ||
+        (ce = cudaMallocAsync(&d_out, sizeof(float) * (size_t)e, s)) != cudaSuccess ||
+        (weighted && (ce = cudaMallocAsync(&d_w, sizeof(float) * (size_t)n, s)) != cudaSuccess)) {
+      st = set_cuda_error(ce);
+      break;
+    }
+    if ((ce = cudaMemcpyAsync(d_rp, row_ptr, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (ce = cudaMemcpyAsync(d_col, col_idx, sizeof(int32_t) * (size_t)e, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (weighted && (ce = cudaMemcpyAsync(d_w, vertex_w, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, s)) != cudaSuccess)) {
+      st = set_cuda_error(ce);
+      break;
+    }
+    const jx_csr g{n, e, d_rp, d_col};
+    if ((st = jx_jaccard(&g, weighted ? d_w : nullptr, d_out, algo, (jx_stream_t)s)) != JX_OK) break;
+    if ((ce = cudaMemcpyAsync(out_j, d_out, sizeof(float) * (size_t)e, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
+      st = set_cuda_error(ce);
+      break;
+    }
+  } while (0);
+  if (d_rp) cudaFreeAsync(d_rp, s);
+  if (d_col) cudaFreeAsync(d_col, s);
+  if (d_out) cudaFreeAsync(d_out, s);
+  if (d_w) cudaFreeAsync(d_w, s);
+  ce = cudaStreamSynchronize(s);
+  if (st == JX_OK && ce != cudaSuccess) st = set_cuda_error(ce);
+  cudaStreamDestroy(s);
+  return st;
+}
+
+} // extern "C"

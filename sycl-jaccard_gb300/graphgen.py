@@ -1,0 +1,110 @@
+"""Synthetic graphs of the shapes the benchmark configurations name.
+
+Binds ``csrc/gen/libjxgen.so`` (host C++/OpenMP).  Every draw is a function of the seed
+only (``csrc/jx_rng.h``), so a graph is identical on any machine and thread count.  All
+graphs are symmetric, self-loop free, deduplicated, with each row sorted ascending -- the
+form the reference's driver hands to the operator (main.cpp:99-120).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_gen = None
+
+
+def _lib():
+    global _gen
+    if _gen is None:
+        if not os.path.exists(_build.LIBGEN):
+            _build.build_generator()
+        L = ctypes.CDLL(_build.LIBGEN)
+        L.jxg_rmat.restype = ctypes.c_void_p
+        L.jxg_rmat.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
+                               ctypes.c_double, ctypes.c_uint64, ctypes.c_int]
+        L.jxg_er_gnp.restype = ctypes.c_void_p
+        L.jxg_er_gnp.argtypes = [ctypes.c_int64, ctypes.c_double, ctypes.c_uint64, ctypes.c_int]
+        L.jxg_er_gnm.restype = ctypes.c_void_p
+        L.jxg_er_gnm.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_uint64, ctypes.c_int]
+        for f in ("jxg_num_vertices", "jxg_num_edges"):
+            getattr(L, f).restype = ctypes.c_int64
+            getattr(L, f).argtypes = [ctypes.c_void_p]
+        L.jxg_export.restype = ctypes.c_int
+        L.jxg_export.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.jxg_free.argtypes = [ctypes.c_void_p]
+        L.jxg_uniform_weights.argtypes = [ctypes.c_int64, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_int]
+        _gen = L
+    return _gen
+
+
+def _take(h):
+    L = _lib()
+    if not h:
+        raise MemoryError("graph generation failed")
+    try:
+        n, e = L.jxg_num_vertices(h), L.jxg_num_edges(h)
+        rp = np.empty(n + 1, np.int32)
+        col = np.empty(e, np.int32)
+        if L.jxg_export(h, rp.ctypes.data, col.ctypes.data) != 0:
+            raise ValueError("graph has 2^31 or more edges; int32 CSR impossible")
+        return rp, col
+    finally:
+        L.jxg_free(h)
+
+
+def rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+         seed: int = 0, threads: int = 0):
+    """R-MAT(scale, edge_factor, a, b, c), symmetrised / deduplicated / loop-free int32 CSR."""
+    return _take(_lib().jxg_rmat(scale, edge_factor, a, b, c, seed, threads))
+
+
+def er_gnp(n: int, p: float, seed: int = 0, threads: int = 0):
+    """Erdos-Renyi G(n, p) (every pair tested; n <= 2^20)."""
+    return _take(_lib().jxg_er_gnp(n, p, seed, threads))
+
+
+def er_gnm(n: int, m: int, seed: int = 0, threads: int = 0):
+    """Erdos-Renyi G(n, m)-style: m uniform undirected samples, symmetrised/deduplicated."""
+    return _take(_lib().jxg_er_gnm(n, m, seed, threads))
+
+
+def uniform_weights(n: int, seed: int = 0, threads: int = 0) -> np.ndarray:
+    """Per-vertex float32 weights uniform on the 2^-24 grid of (0, 1]."""
+    out = np.empty(n, np.float32)
+    _lib().jxg_uniform_weights(n, seed, out.ctypes.data, threads)
+    return out
+
+
+def stats(row_ptr: np.ndarray, col: np.ndarray) -> dict:
+    """V, E, degree facts and sum_e min(d_u, d_v) (the byte model's must-read term)."""
+    n = len(row_ptr) - 1
+    deg = np.diff(row_ptr).astype(np.int64)
+    # per-edge min(d_u, d_v) without materialising an int64 copy of the source array
+    sum_min = 0
+    step = 1 << 20
+    for s in range(0, n, step):
+        e0, e1 = int(row_ptr[s]), int(row_ptr[min(n, s + step)])
+        src_deg = np.repeat(deg[s:min(n, s + step)], deg[s:min(n, s + step)])
+        sum_min += int(np.minimum(src_deg, deg[col[e0:e1]]).sum())
+    return {"V": int(n), "E": int(len(col)), "isolated": int((deg == 0).sum()),
+            "max_degree": int(deg.max()) if n else 0, "sum_min": int(sum_min)}
+
+
+# Named configurations (the benchmark's workload shapes).
+def config_graph(name: str, threads: int = 0):
+    """Returns (row_ptr, col_idx, vertex_weights or None, description)."""
+    if name == "er4096":
+        rp, col = er_gnp(4096, 16.0 / 4095.0, seed=1, threads=threads)
+        return rp, col, np.ones(4096, np.float32), "ER G(4096, 16/4095) seed 1, unit weights"
+    if name == "rmat20":
+        rp, col = rmat(20, 16, 0.57, 0.19, 0.19, seed=2, threads=threads)
+        return rp, col, None, "RMAT scale 20 ef 16 (.57,.19,.19,.05) seed 2, unweighted"
+    if name == "rmat24w":
+        rp, col = rmat(24, 16, 0.57, 0.19, 0.19, seed=3, threads=threads)
+        w = uniform_weights(len(rp) - 1, seed=4, threads=threads)
+        return rp, col, w, "RMAT scale 24 ef 16 (.57,.19,.19,.05) seed 3, vertex weights U(0,1] seed 4"
+    raise KeyError(name)

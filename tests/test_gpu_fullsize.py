@@ -1,0 +1,63 @@
+"""GPU: a full-size skewed configuration (RMAT scale 20, ef 16, seed 2) checked through
+size-independent properties plus oracle spot checks on sampled rows, including the hubs."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def rmat20(jx):
+    rp, col, _, _ = jx.graphgen.config_graph("rmat20")
+    return rp, col
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def test_rmat20_properties_and_samples(jx, O, rmat20):
+    import torch
+    rp, col = rmat20
+    g = jx.GraphCSRView.from_numpy(rp, col)
+    J = jx.jaccard(g).cpu().numpy()
+    Jec = jx.jaccard(g, edge_centric=True).cpu().numpy()
+    torch.cuda.synchronize()
+    n = len(rp) - 1
+    d = np.diff(rp).astype(np.int64)
+    src = np.repeat(np.arange(n, dtype=np.int64), d)
+    # EC and VC unweighted agree bit for bit (J = c / (du + dv - c) both ways)
+    assert np.array_equal(bits(J), bits(Jec))
+    # range and symmetry: J(u,v) == J(v,u) bitwise
+    assert np.all((J >= 0) & (J <= 1))
+    order = np.lexsort((src, col))  # edges sorted by (col, src) = reverse-edge order
+    assert np.array_equal(bits(J[order]), bits(J))
+    # recovered counts are integers <= min(du, dv)
+    dsum = (d[src] + d[col]).astype(np.float64)
+    c = J.astype(np.float64) * dsum / (1 + J.astype(np.float64))
+    assert np.all(np.abs(c - np.round(c)) < 1e-3)
+    assert np.all(np.round(c) <= np.minimum(d[src], d[col]))
+    # oracle on sampled rows: the biggest hubs, a middle band and the tail
+    hubs = np.argsort(-d)[:3]
+    rows = [(int(h), int(h) + 1) for h in hubs] + [(n // 2, n // 2 + 2000), (n - 3000, n)]
+    for r0, r1 in rows:
+        want = O.jaccard(rp, col, None, rows=(r0, r1))
+        assert np.array_equal(bits(J[rp[r0]:rp[r1]]), bits(want)), (r0, r1)
+
+
+def test_rmat20_weighted_samples(jx, O, rmat20):
+    import torch
+    rp, col = rmat20
+    n = len(rp) - 1
+    w = jx.graphgen.uniform_weights(n, seed=4)
+    g = jx.GraphCSRView.from_numpy(rp, col)
+    J = jx.jaccard(g, torch.from_numpy(w).cuda()).cpu().numpy()
+    d = np.diff(rp)
+    hubs = np.argsort(-d)[:2]
+    S = O.rowsum(rp, col, w)
+    for r0, r1 in [(int(h), int(h) + 1) for h in hubs] + [(n // 3, n // 3 + 3000)]:
+        want = np.empty(int(rp[r1] - rp[r0]), np.float32)
+        O.lib().jxo_jaccard_rows(0, n, rp.ctypes.data_as(O._I32), col.ctypes.data_as(O._I32),
+                                 w.ctypes.data_as(O._F32), r0, r1, S.ctypes.data_as(O._F32),
+                                 want.ctypes.data_as(O._F32), 0)
+        assert np.array_equal(bits(J[rp[r0]:rp[r1]]), bits(want)), (r0, r1)
