@@ -1,0 +1,409 @@
+"""Benchmark: edges scored per second by the fused Jaccard operator on one GB300.
+
+Workload (default): the large weighted configuration -- R-MAT scale 24, edge factor 16,
+(a,b,c,d) = (.57,.19,.19,.05), seed 3, symmetrised / deduplicated / loop-free int32 CSR, with
+per-vertex float32 weights uniform in (0,1] (seed 4); vertex-centric weighted Jaccard for
+every stored edge.  Synthetic data of the named shape (there is no dataset).
+
+A step is one call of the operator (``jx_jaccard_ws``) over the whole graph, resident in
+HBM.  The graph (2.2 GB) is far larger than L2 (129 MB), so no L2 flush is needed between
+steps.  Timing: W warm-up steps, then K steps between a barrier + synchronize on both sides,
+CUDA events on the launching stream, max over ranks.  ``e2e`` times the host-buffer entry
+point (``jx_jaccard_host``): pinned host arrays in, results out, copies inside the timed
+region.  ``cpu_baseline`` times the reference's own kernels (through the host SYCL subset)
+on a bounded, evenly spread sample of work-groups, on this machine's host cores.
+
+``--impl reference`` runs only that CPU reference arm and prints its own line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+METRIC = "edges scored/s"
+UNIT = "edges/s"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def byte_model(V, E, sum_min, weighted):
+    """Designated algorithmic bytes of one operator call (per-edge must-read model)."""
+    b = 4 * (V + 1) + 16 * E + 4 * sum_min
+    if weighted:
+        b += 4 * (V + 1) + 8 * E + 4 * V + 4 * E
+    return b
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_FILE) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if p[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_graph(name, threads):
+    jx = importlib.import_module("sycl-jaccard_gb300")
+    t = time.time()
+    rp, col, w, desc = jx.graphgen.config_graph(name, threads=threads)
+    st = jx.graphgen.stats(rp, col)
+    log(f"graph {name}: V={st['V']} E={st['E']} max_deg={st['max_degree']} sum_min={st['sum_min']:.4g} "
+        f"({time.time() - t:.1f}s)")
+    return rp, col, w, desc, st
+
+
+# ------------------------------------------------------------------ CPU reference arm
+
+def sampled_rows(n, K, r):
+    """Rows the reference's IS kernel processes when only work-groups g % K == r run.
+
+    Jaccard_IsKernel::invoke (jaccard.cpp:414-418) uses groups of 8 rows and a grid of
+    min(ceil(n/8), 65535) groups with a row grid-stride, so row x belongs to group
+    ((x mod G0) // 8) with G0 = 8 * min(ceil(n/8), 65535).
+    """
+    G0 = 8 * min((n + 7) // 8, 65535)
+    x = np.arange(n, dtype=np.int64)
+    return ((x % G0) // 8) % K == r
+
+
+def row_work(rp, col):
+    """Per-row cost proxy of the reference's IS kernel: sum over the row's edges of
+    min(d_u, d_v) * (1 + log2(max(d_u, d_v))) (binary searches of the shorter list)."""
+    n = len(rp) - 1
+    d = np.diff(rp.astype(np.int64))
+    work = np.zeros(n, np.float64)
+    step = 1 << 20
+    for s in range(0, n, step):
+        e0, e1 = int(rp[s]), int(rp[min(n, s + step)])
+        du = np.repeat(d[s:min(n, s + step)], d[s:min(n, s + step)])
+        dv = d[col[e0:e1]]
+        c = np.minimum(du, dv) * (1.0 + np.log2(np.maximum(np.maximum(du, dv), 1)))
+        rows = np.repeat(np.arange(s, min(n, s + step)), d[s:min(n, s + step)])
+        work += np.bincount(rows, weights=c, minlength=n)
+    return work
+
+
+def cpu_reference(rp, col, w, target_s=20.0):
+    """Time the reference (through the host SYCL subset) on a bounded work-group sample.
+
+    Fixed per-call cost `a` (the reference allocates 12E + 4V bytes of temporaries per call,
+    jaccard.cpp:931-934) is timed with a sample that runs no work-group.  Then every K-th
+    work-group (residue K/2, evenly spread over the row range through the kernels' grid
+    strides) runs; K is chosen for about target_s seconds.  The whole-graph call time is
+    extrapolated by the sampled share of the IS kernel's work (row_work):
+        T = a + (t_K - a) * W_total / W_sampled,   reported rate = E / T.
+    """
+    from oracle import oracle as O
+    kind = "reference"
+    try:
+        L = O.ref_lib()
+    except Exception as exc:  # build failure on this machine
+        log(f"reference build unavailable: {exc}")
+        L = None
+    threads = os.cpu_count() or 1
+    n, E = len(rp) - 1, len(col)
+    work = row_work(rp, col)
+    W = work.sum()
+
+    def timed(K, r):
+        t0 = time.perf_counter()
+        if kind == "reference":
+            O.ref_jaccard(rp, col, w, edge_centric=False, threads=threads, group_sample=K, group_residue=r)
+        else:
+            rows = (r, min(n, r + max(1, n // K)))
+            O.jaccard(rp, col, w, rows=rows, threads=threads)
+        return time.perf_counter() - t0
+
+    if L is None:
+        kind = "port"
+    if kind == "reference":
+        a = timed(1 << 40, (1 << 40) - 1)
+        share = lambda K: work[sampled_rows(n, K, K // 2)].sum() / W
+    else:
+        a = 0.0
+        share = lambda K: work[K // 2: min(n, K // 2 + max(1, n // K))].sum() / W
+    K = 4096
+    t_cal = timed(K, K // 2)
+    full = max(t_cal - a, 1e-4) / max(share(K), 1e-12)
+    K = 1
+    while K < (1 << 20) and full * share(K * 2) >= target_s:
+        K *= 2
+    while K > 1 and full * share(K) < target_s / 2:
+        K //= 2
+    t = timed(K, K // 2)
+    sh = share(K)
+    T = a + max(t - a, 1e-6) / max(sh, 1e-12)
+    if kind == "reference":
+        sel = sampled_rows(n, K, K // 2)
+        edges = int(np.diff(rp.astype(np.int64))[sel].sum())
+        sample = (f"reference jaccard.cpp (VC{' weighted' if w is not None else ''}) via host SYCL "
+                  f"subset, work-groups g % {K} == {K // 2} of each kernel ({edges} of {E} edges, "
+                  f"{sh:.2e} of the IS work), {threads} threads; fixed per-call cost {a:.2f}s + "
+                  f"sampled {t - a:.2f}s, extrapolated to the whole graph by work share")
+    else:
+        sample = f"C restatement (oracle port), a row range with {sh:.2e} of the work, {threads} threads"
+    return {"value": E / T, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample,
+            "seconds": round(a + t + t_cal, 3), "extrapolated_call_s": round(T, 2)}
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def run_gpu(args, world, rank, local):
+    import torch
+    jx = importlib.import_module("sycl-jaccard_gb300")
+    torch.cuda.set_device(local)
+    threads = os.cpu_count() or 1
+    rp, col, w, desc, st = make_graph(args.workload, threads)
+    V, E = st["V"], st["E"]
+    weighted = w is not None and not args.ec
+    g = jx.GraphCSRView.from_numpy(rp, col, device=f"cuda:{local}")
+    wd = torch.from_numpy(w).cuda() if weighted else None
+    out = torch.empty(E, dtype=torch.float32, device="cuda")
+    ws = torch.empty(jx.workspace_size(g, weighted, args.ec), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        jx.jaccard(g, wd, out, edge_centric=args.ec, workspace=ws)
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    jx.launch_count_reset()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            jx.jaccard(g, wd, out, edge_centric=args.ec, workspace=ws)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = jx.launch_count()
+    barrier(world)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = max_over_ranks(ms, world)
+    clocks = clk.summary()
+
+    # per-launch breakdown of one extra (untimed) step
+    jx.lib().jx_profile_begin()
+    jx.jaccard(g, wd, out, edge_centric=args.ec, workspace=ws)
+    buf = ctypes.create_string_buffer(4096)
+    jx.lib().jx_profile_end(buf, 4096)
+    kernels = {}
+    for item in buf.value.decode().split(";"):
+        if "=" in item:
+            k, v = item.split("=")
+            kernels[k] = round(float(v), 4)
+    ksum = sum(kernels.values()) or 1.0
+    dominant = max(kernels, key=kernels.get) if kernels else None
+
+    # end-to-end through the host-buffer C-ABI entry point (pinned host memory)
+    e2e = None
+    if not args.no_e2e:
+        h_rp = torch.from_numpy(rp).pin_memory()
+        h_col = torch.from_numpy(col).pin_memory()
+        h_w = torch.from_numpy(w).pin_memory() if weighted else None
+        h_out = torch.empty(E, dtype=torch.float32).pin_memory()
+        L = jx.lib()
+        algo = 1 if args.ec else 0
+        call = lambda: L.jx_jaccard_host(V, E, h_rp.data_ptr(), h_col.data_ptr(),
+                                         h_w.data_ptr() if h_w is not None else None,
+                                         h_out.data_ptr(), algo)
+        for _ in range(min(2, args.warmup)):
+            assert call() == 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            rc = call()
+            assert rc == 0, rc
+        t1 = time.perf_counter()
+        e2e_s = (t1 - t0) / args.e2e_steps
+        e2e_s = max_over_ranks(e2e_s, world)
+        h2d = 4 * (V + 1) + 4 * E + (4 * V if weighted else 0)
+        e2e = {"value": E * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": 4 * E, "ms_per_step": round(e2e_s * 1e3, 3),
+               "timing": "host wall clock around the synchronous call"}
+        out_host = h_out.numpy()
+        dev = out.cpu().numpy()
+        if not np.array_equal(out_host.view(np.uint32), dev.view(np.uint32)):
+            raise AssertionError("host-buffer entry point disagrees with the device path")
+
+    B = byte_model(V, E, st["sum_min"], weighted)
+    peak, peak_kind = hbm_peak()
+    achieved = B / (ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                "kernel": "fused operator (one jx_jaccard_ws call = plan, rowsum, sentinel fill, "
+                          "hub/CTA/warp row kernels, fix-up)",
+                "algorithmic_bytes": B,
+                "dominant_launch": dominant,
+                "dominant_share": round(kernels.get(dominant, 0.0) / ksum, 4) if dominant else None}
+    result = {
+        "metric": METRIC, "value": E * world / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {desc}", "algorithm": "edge_centric" if args.ec else "vertex_centric",
+                   "weighted": weighted, "V": V, "E": E, "sum_min": st["sum_min"],
+                   "max_degree": st["max_degree"], "l2": "inputs (2.2 GB) larger than L2; no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
+        "kernels_ms": kernels,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            result["cpu_baseline"] = cpu_reference(rp, col, w if weighted else None, args.cpu_seconds)
+        except Exception as exc:
+            result["cpu_baseline"] = {"value": None, "error": str(exc)[:200]}
+    return result
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    rp, col, w, desc, st = make_graph(args.workload, threads)
+    weighted = w is not None and not args.ec
+    vals = []
+    cb = None
+    for i in range(args.warmup + args.steps):
+        cb = cpu_reference(rp, col, w if weighted else None, args.cpu_seconds / max(1, args.steps))
+        if i >= args.warmup:
+            vals.append(cb["value"])
+    value = statistics.median(vals)
+    cb["value"] = value
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(st["E"] / value * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"{args.workload}: {desc}", "algorithm": "vertex_centric",
+                       "weighted": weighted, "V": st["V"], "E": st["E"], "sum_min": st["sum_min"]},
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="jx", choices=["jx", "reference"])
+    ap.add_argument("--workload", default="rmat24w", choices=["rmat24w", "rmat20", "er4096"])
+    ap.add_argument("--ec", action="store_true", help="edge-centric algorithm")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "jx":
+        log("warm-up raised to 3 steps")
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        res = run_reference(args, world, rank)
+    else:
+        res = run_gpu(args, world, rank, local)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+
+
+if __name__ == "__main__":
+    main()

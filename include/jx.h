@@ -144,6 +144,13 @@ jx_status jx_ec_unweighted(int32_t e, int32_t n, const int32_t *row_ptr, const i
  * Synchronous on `stream`. */
 jx_status jx_csr_check(const jx_csr *g, uint32_t *flags, jx_stream_t stream);
 
+/* Per-launch timing of the fused operator on this thread: jx_profile_begin() starts
+ * recording an event after each kernel the operator launches; jx_profile_end() waits for
+ * them and writes "name=ms;name=ms;..." into buf (NUL-terminated, truncated to len).
+ * Returns the number of timed launches.  Diagnostic only; adds event records to the stream. */
+void jx_profile_begin(void);
+int jx_profile_end(char *buf, size_t len);
+
 /* Number of kernels this library launched on this thread since the last reset. */
 uint64_t jx_launch_count(void);
 void jx_launch_count_reset(void);

@@ -63,7 +63,7 @@ def ref_lib():
                 return None
         L = ctypes.CDLL(so)
         L.jxref_set_threads.argtypes = [ctypes.c_int]
-        L.jxref_set_group_sample.argtypes = [ctypes.c_int]
+        L.jxref_set_group_sample.argtypes = [ctypes.c_longlong, ctypes.c_longlong]
         L.jxref_jaccard.argtypes = [ctypes.c_int, ctypes.c_int32, ctypes.c_int32, _I32, _I32, _F32,
                                     _F32]
         L.jxref_rowsum.argtypes = [ctypes.c_int32, ctypes.c_int32, _I32, _I32, _F32, _F32]
@@ -132,19 +132,22 @@ def jaccard_f64(row_ptr, col, w=None, rows=None, threads=0):
 
 # ---------------------------------------------------------------- reference (via SYCL subset)
 
-def ref_jaccard(row_ptr, col, w=None, edge_centric=False, threads=0, group_sample=1):
+def ref_jaccard(row_ptr, col, w=None, edge_centric=False, threads=0, group_sample=1,
+                group_residue=0):
+    """Run sygraph::jaccard of the reference; with group_sample=K only work-groups whose id is
+    group_residue modulo K execute (a timing sample: the results are then incomplete)."""
     L = ref_lib()
     if L is None:
         raise RuntimeError("reference sources unavailable")
     L.jxref_set_threads(threads)
-    L.jxref_set_group_sample(group_sample)
+    L.jxref_set_group_sample(group_sample, group_residue)
     n = len(row_ptr) - 1
     out = np.zeros(len(col), np.float32)
     try:
         L.jxref_jaccard(1 if edge_centric else 0, n, len(col), _p(row_ptr, _I32), _p(col, _I32),
                         _p(w, _F32), _p(out, _F32))
     finally:
-        L.jxref_set_group_sample(1)
+        L.jxref_set_group_sample(1, 0)
     return out
 
 

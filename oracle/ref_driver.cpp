@@ -52,8 +52,9 @@ void jxref_set_threads(int n) {
 #endif
 }
 
-/* Execute only every k-th work-group of each launch (timing samples); 1 = everything. */
-void jxref_set_group_sample(int k) { jxshim::set_group_sample(k); }
+/* Execute only work-groups g with g % k == residue in each launch (timing samples);
+ * k = 1 runs everything. */
+void jxref_set_group_sample(long long k, long long residue) { jxshim::set_group_sample(k, residue); }
 
 int jxref_jaccard(int edge_centric, int32_t n, int32_t e, const int32_t *row_ptr,
                   const int32_t *col, const float *vertex_w, float *out) {

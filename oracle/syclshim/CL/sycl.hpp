@@ -50,9 +50,14 @@
 #endif
 
 namespace jxshim {
-/* Group sampling stride; 1 = run every work-group.  Defined in syclshim.cpp. */
-extern int g_group_sample;
-inline void set_group_sample(int k) { g_group_sample = k > 0 ? k : 1; }
+/* Group sampling: run only work-groups whose linear id g has g % stride == residue.
+ * stride 1 = run every work-group.  Defined in syclshim.cpp. */
+extern long long g_group_sample;
+extern long long g_group_residue;
+inline void set_group_sample(long long k, long long residue = 0) {
+  g_group_sample = k > 0 ? k : 1;
+  g_group_residue = residue;
+}
 } // namespace jxshim
 
 namespace cl {
@@ -324,7 +329,7 @@ public:
       total_groups *= ngroups[i];
       items *= r.l.v[i];
     }
-    const int stride = jxshim::g_group_sample;
+    const long long stride = jxshim::g_group_sample, residue = jxshim::g_group_residue;
     const size_t arena = local_bytes > 0 ? local_bytes : 64;
     auto run_one = [&](size_t glin, bool fibers, char *base) -> bool {
       size_t grp[D];
@@ -353,15 +358,18 @@ public:
       return detail::run_group(items, item, fibers);
     };
     if (total_groups == 0) return;
-    /* First group decides whether fibers are needed. */
+    /* The first executed group decides whether fibers are needed. */
+    long long g0 = 0;
+    while (g0 < (long long)total_groups && g0 % stride != residue) ++g0;
+    if (g0 >= (long long)total_groups) return;
     std::vector<char> first(arena);
-    const bool fibers = run_one(0, true, first.data());
+    const bool fibers = run_one((size_t)g0, true, first.data());
 #pragma omp parallel
     {
       std::vector<char> local(arena);
 #pragma omp for schedule(dynamic, 1)
-      for (long long g = 1; g < (long long)total_groups; ++g) {
-        if ((size_t)g % (size_t)stride != 0) continue;
+      for (long long g = g0 + 1; g < (long long)total_groups; ++g) {
+        if (g % stride != residue) continue;
         run_one((size_t)g, fibers, local.data());
       }
     }

@@ -18,7 +18,8 @@
 #include <setjmp.h>
 
 namespace jxshim {
-int g_group_sample = 1;
+long long g_group_sample = 1;
+long long g_group_residue = 0;
 }
 
 namespace cl {

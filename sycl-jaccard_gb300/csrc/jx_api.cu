@@ -2,7 +2,10 @@
 // the CSR validator.
 #include "jx_common.cuh"
 
+#include <cstdio>
+#include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
 namespace jx {
@@ -16,6 +19,21 @@ jx_status set_cuda_error(cudaError_t e) {
 }
 
 void count_launches(uint64_t k) { tl_launches += k; }
+
+struct ProfMark {
+  const char *name;
+  cudaEvent_t ev;
+};
+static thread_local bool tl_prof = false;
+static thread_local std::vector<ProfMark> tl_marks;
+
+void prof_mark(const char *name, cudaStream_t s) {
+  if (!tl_prof) return;
+  cudaEvent_t ev;
+  if (cudaEventCreate(&ev) != cudaSuccess) return;
+  cudaEventRecord(ev, s);
+  tl_marks.push_back({name, ev});
+}
 
 int sm_count() {
   static std::mutex mu;
@@ -100,6 +118,35 @@ const char *jx_status_string(jx_status s) {
 }
 
 int jx_version(void) { return 10000; }
+
+void jx_profile_begin(void) {
+  for (auto &m : tl_marks) cudaEventDestroy(m.ev);
+  tl_marks.clear();
+  tl_prof = true;
+}
+
+int jx_profile_end(char *buf, size_t len) {
+  tl_prof = false;
+  std::string out;
+  int count = 0;
+  for (size_t i = 1; i < tl_marks.size(); ++i) {
+    float ms = 0.0f;
+    cudaEventSynchronize(tl_marks[i].ev);
+    if (cudaEventElapsedTime(&ms, tl_marks[i - 1].ev, tl_marks[i].ev) != cudaSuccess) continue;
+    char line[160];
+    snprintf(line, sizeof line, "%s%s=%.6f", count ? ";" : "", tl_marks[i].name, ms);
+    out += line;
+    ++count;
+  }
+  for (auto &m : tl_marks) cudaEventDestroy(m.ev);
+  tl_marks.clear();
+  if (buf && len) {
+    size_t k = out.size() < len - 1 ? out.size() : len - 1;
+    memcpy(buf, out.data(), k);
+    buf[k] = 0;
+  }
+  return count;
+}
 int jx_last_cuda_error(void) { return tl_last_cuda; }
 uint64_t jx_launch_count(void) { return tl_launches; }
 void jx_launch_count_reset(void) { tl_launches = 0; }

@@ -28,6 +28,11 @@ inline jx_status check_launch() {
 }
 int sm_count();
 
+// Optional per-launch timing (jx_profile_begin / jx_profile_end): when enabled on this
+// thread, prof_mark records an event on `s` after a launch; durations are the gaps between
+// consecutive marks.  A no-op when disabled.
+void prof_mark(const char *name, cudaStream_t s);
+
 // -------------------------------------------------------------- device helpers
 
 // Binary search of `key` in col[left .. right] (inclusive), jaccard.cpp:353-367.

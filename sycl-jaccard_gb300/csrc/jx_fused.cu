@@ -1,50 +1,69 @@
 // Fused Jaccard operator: intersection and weight in one pass, J written once per edge, no
 // atomics on results.  Drop-in for sygraph::jaccard<edge_centric> (jaccard.cpp:926-955).
 //
-// Work decomposition ("tasks").  An intersection |N(x) n N(y)| is computed by staging the
-// longer list N(u) in shared memory as an open-addressing hash set and streaming the shorter
-// list N(v) through it.  Row u (the "cur" list) owns a task for every neighbour v with
-// d_v <= d_u (v's list is the "ref" list, the one the reference walks element by element).
-// The reference picks the ref list per directed edge (VC: jaccard.cpp:333-336, EC:
-// jaccard.cpp:716-719), so one task serves two directed edges:
+// Work decomposition ("tasks").  An intersection is computed by staging the longer list
+// N(u) as a membership structure and streaming the shorter list N(v) through it.  Row u
+// owns a task for every neighbour v with d_v <= d_u; v's list is the "ref" list, the one the
+// reference walks element by element.  The reference picks the ref list per directed edge
+// (VC: jaccard.cpp:333-336, EC: jaccard.cpp:716-719), so one task serves two directed edges:
 //   VC: (u,v) always (ref = v when d_u >= d_v);      (v,u) when d_v < d_u
 //   EC: (u,v) when d_v < d_u;                         (v,u) always (ref = v when d_v <= d_u)
-// The reverse edge (v,u) is located for free: it is the position of u inside N(v), which
-// the task streams anyway.  Its result is bit-identical because both edges use the same ref
-// list, the same cur set and a commutative S_u + S_v.  Edges that no task covers (graphs
-// that are not symmetric) keep a sentinel and are computed by a fix-up pass.
+// The reverse edge (v,u) is found for free: it is the position of u inside N(v), which the
+// task streams anyway.  Its result is bit-identical: same ref list, same cur set, and a
+// commutative S_u + S_v.  Edges no task covers (graphs that are not symmetric, repeated
+// neighbours) keep a sentinel and are computed by the fix-up pass.
 //
-// Degree bins (by d_u, the staged list):
-//   B0: d_u <= 32        one warp per row, 64-slot table per warp
-//   B1: d_u <= 512       one warp per row, 1024-slot table per warp
-//   B2: d_u <= 24576     one 1024-thread CTA per row, table of 2*d_u slots (<= 192 KB)
-//   B3: larger (hubs)    one CTA per row, ref elements binary-searched in N(u)
+// Bins by d_u (the staged list), each row list sorted by degree, largest first:
+//   B0  d_u <= 32      one warp per row, one lane per task, 64-slot hash per warp
+//   B1  d_u <= 512     one warp per row, 1024-slot hash per warp (shared memory)
+//   B2  d_u <= 24576   one 1024-thread CTA per row, hash of up to 48K slots (192 KB)
+//   hub d_u >  24576   8-CTA clusters; N(u) as a bitmap over [0, n) in global memory (L2)
 //
-// Weighted sums follow the reference's accumulation order exactly: ref positions are taken
-// in the order il, il+8, il+16, ... for il = 0..7 (jaccard.cpp:343) and folded one by one.
+// Streaming: a warp reads the ref list in 256-element chunks, lane k holding positions
+// k + 32j (j = 0..7): eight independent coalesced loads in flight per lane.
+//
+// Weighted sums follow the reference's accumulation order exactly.  On a CPU SYCL device its
+// 8 i-lanes add their matches one lane after another (jaccard.cpp:343, 370-396): ref
+// positions 0, 8, 16, ..., then 1, 9, 17, ..., i.e. "class" c = position mod 8 major,
+// position minor.  Class 0 is folded while streaming; the matched values of classes 1..7 are
+// appended to per-warp class streams (shared memory for B1, global scratch otherwise) and
+// folded class by class after the list ends.  A task whose class stream would overflow is
+// recomputed with a class-major strided walk (same order, no buffering).
 #include "jx_common.cuh"
+
+#include <cooperative_groups.h>
 
 #include <algorithm>
 
+namespace cg = cooperative_groups;
+
 namespace jx {
 
-constexpr int kBins = 4;
 constexpr int32_t kB0Max = 32, kB1Max = 512, kB2Max = 24576;
-constexpr int kB0Slots = 64, kB1Slots = 1024;
+constexpr int kB0Slots = 64, kB1Slots = 1024, kB2Slots = 49152;
 constexpr int kB2Threads = 1024;
-constexpr int kRowThreads = 256; // warps-per-row kernels
+constexpr int kRowThreads = 256;
+constexpr int kHubThreads = 1024;
+constexpr int kCluster = 8;
 constexpr int32_t kEmpty = -1;
+constexpr int kChunk = 256;
+constexpr int kB1Cap = kB1Max / 8;   // class-stream capacity per class, B1 (exact bound)
+constexpr int kCap = 2048;           // class-stream capacity per class, B2 / hubs
+constexpr int kHubTasksPerUnit = 32768;
+constexpr int kKeys = 128;           // plan sort keys: 4 bins x 32 log2 buckets
+constexpr unsigned kClass0 = 0x01010101u;
 
-// Counters in the workspace (int32 each).
-enum { kCntBin0 = 0, kWorkBin2 = kBins, kWorkBin3 = kBins + 1, kCounters = 16 };
-
-struct Workspace {
-  float *S;        // weighted row sums, n floats (weighted VC only)
-  int32_t *rows;   // bin row lists: bin b starts at rows + b * n ... packed by offsets below
-  int32_t *cnt;    // counters
+// Counters in the workspace (int32).
+enum {
+  kCntKeys = 0,                // [0, 128)   per-key counts, then cursors
+  kOffKeys = kKeys,            // [128, 257) key offsets (exclusive scan, 129 entries)
+  kCtrB2 = 2 * kKeys + 8,      // work counter, B2 rows
+  kCtrHub,                     // work counter, hub units
+  kNumHubUnits,                // number of hub units
+  kCounters = 2 * kKeys + 32
 };
 
-// ---------------------------------------------------------------- hash set in shared memory
+// ---------------------------------------------------------------- membership probes
 __device__ __forceinline__ uint32_t hslot(int32_t key, uint32_t size) {
   return __umulhi((uint32_t)key * 0x9E3779B1u, size);
 }
@@ -58,83 +77,158 @@ __device__ __forceinline__ void hset_insert(int32_t *t, uint32_t size, int32_t k
   }
 }
 
-__device__ __forceinline__ bool hset_find(const int32_t *t, uint32_t size, int32_t key) {
-  uint32_t s = hslot(key, size);
-  for (;;) {
-    const int32_t k = t[s];
-    if (k == key) return true;
-    if (k == kEmpty) return false;
-    if (++s == size) s = 0;
-  }
-}
-
+// Open-addressing hash set of N(u) in shared memory (load factor <= 1/2: every probe loop
+// ends at an empty slot).
 struct HashProbe {
   const int32_t *t;
   uint32_t size;
-  __device__ bool operator()(int32_t key) const { return hset_find(t, size, key); }
+  __device__ __forceinline__ bool operator()(int32_t key) const {
+    uint32_t s = hslot(key, size);
+    for (;;) {
+      const int32_t k = t[s];
+      if (k == key) return true;
+      if (k == kEmpty) return false;
+      if (++s == size) s = 0;
+    }
+  }
 };
 
-struct SearchProbe { // sorted cur list in global memory (hub fallback)
+// Bitmap of N(u) over [0, n) in global memory, rebuilt per hub: read through L2 only
+// (ld.global.cg), never from a possibly stale L1 line.
+struct BitmapProbe {
+  const uint32_t *bm;
+  __device__ __forceinline__ bool operator()(int32_t key) const {
+    return (__ldcg(bm + (key >> 5)) >> (key & 31)) & 1u;
+  }
+};
+
+// Sorted cur list in global memory (fix-up path).
+struct SearchProbe {
   const int32_t *col;
-  int32_t lo, hi; // inclusive range
-  __device__ bool operator()(int32_t key) const { return bsearch_found(col, lo, hi, key); }
+  int32_t lo, hi; // inclusive
+  __device__ __forceinline__ bool operator()(int32_t key) const { return bsearch_found(col, lo, hi, key); }
+};
+
+// ---------------------------------------------------------------- class streams
+// Per-warp storage for the matched values of classes 1..7 (class c at base + (c-1)*cap).
+struct ClassStreams {
+  float *base;
+  int cap;
+  __device__ __forceinline__ void put(int c, int pos, float v) const {
+    if (pos < cap) __stcg(base + (c - 1) * cap + pos, v);
+  }
+  __device__ __forceinline__ float get(int c, int pos) const { return __ldcg(base + (c - 1) * cap + pos); }
+};
+
+struct SmemClassStreams {
+  float *base;
+  int cap;
+  __device__ __forceinline__ void put(int c, int pos, float v) const {
+    if (pos < cap) base[(c - 1) * cap + pos] = v;
+  }
+  __device__ __forceinline__ float get(int c, int pos) const { return base[(c - 1) * cap + pos]; }
 };
 
 // ---------------------------------------------------------------- one task, one warp
-// Streams N(v) (positions [vs, vs+dv)) through `probe` (membership in N(u)).
-// Returns the reference-order intersection value (count for unweighted) and the position
-// of u inside N(v) (or -1; -2 when u occurs more than once).
+// Class-major strided walk (the reference's order with no buffering); used for overflowing
+// weighted tasks and by the fix-up pass.
 template <bool kWeighted, class Probe>
-__device__ __forceinline__ float warp_task(const Probe &probe, const int32_t *__restrict__ col,
-                                           const float *__restrict__ w, int32_t u, int32_t vs,
-                                           int32_t dv, int32_t &mirror) {
+__device__ __forceinline__ float task_strided(const Probe &probe, const int32_t *__restrict__ col,
+                                              const float *__restrict__ w, int32_t u, int32_t vs,
+                                              int32_t dv, int32_t &mirror) {
   const int lane = threadIdx.x & 31;
   mirror = -1;
-  if (!kWeighted) {
-    int32_t cnt = 0;
-    for (int32_t p0 = 0; p0 < dv; p0 += 32) {
-      const int32_t p = p0 + lane;
+  float acc = 0.0f;
+  for (int il = 0; il < kIsILanes; ++il) {
+    const int32_t cntc = dv > il ? (dv - il + kIsILanes - 1) / kIsILanes : 0;
+    for (int32_t m0 = 0; m0 < cntc; m0 += 32) {
+      const int32_t m = m0 + lane;
       int32_t x = kEmpty;
       bool found = false;
-      if (p < dv) {
-        x = __ldg(col + vs + p);
+      float val = 1.0f;
+      if (m < cntc) {
+        x = __ldg(col + vs + il + kIsILanes * m);
         found = probe(x);
+        if (kWeighted && found) val = __ldg(w + x);
       }
-      cnt += __popc(__ballot_sync(kFull, found));
-      const unsigned mb = __ballot_sync(kFull, x == u);
-      if (mb) mirror = (mirror == -1 && __popc(mb) == 1) ? p0 + __ffs(mb) - 1 : -2;
+      acc = warp_ordered_fold(__ballot_sync(kFull, found), val, acc);
+      const unsigned mb = __ballot_sync(kFull, x == u && x != kEmpty);
+      if (mb) mirror = (mirror == -1 && __popc(mb) == 1) ? il + kIsILanes * (m0 + __ffs(mb) - 1) : -2;
     }
-    return (float)cnt;
-  } else {
-    float acc = 0.0f;
-    for (int il = 0; il < kIsILanes; ++il) {
-      const int32_t cntc = dv > il ? (dv - il + kIsILanes - 1) / kIsILanes : 0;
-      for (int32_t m0 = 0; m0 < cntc; m0 += 32) {
-        const int32_t m = m0 + lane;
-        int32_t x = kEmpty;
-        bool found = false;
-        float val = 0.0f;
-        if (m < cntc) {
-          x = __ldg(col + vs + il + kIsILanes * m);
-          found = probe(x);
-          if (found) val = __ldg(w + x);
-        }
-        acc = warp_ordered_fold(__ballot_sync(kFull, found), val, acc);
-        const unsigned mb = __ballot_sync(kFull, x == u);
-        if (mb) mirror = (mirror == -1 && __popc(mb) == 1) ? il + kIsILanes * (m0 + __ffs(mb) - 1) : -2;
-      }
-    }
-    return acc;
   }
+  return acc;
 }
 
-// Result for a task and the two directed edges it may serve.
+// Chunked stream of N(v) = col[vs, vs+dv) through `probe`.  Returns the intersection value in
+// the reference's order (count when unweighted) and the position of u in N(v) in `mirror`
+// (-1 absent, -2 more than once).
+template <bool kWeighted, class Probe, class Streams>
+__device__ __forceinline__ float task_stream(const Probe &probe, const int32_t *__restrict__ col,
+                                             const float *__restrict__ w, int32_t u, int32_t vs,
+                                             int32_t dv, int32_t &mirror, const Streams &cls) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const int my_class = lane & 7;
+  const unsigned my_cmask = kClass0 << my_class;
+  mirror = -1;
+  int32_t cnt = 0;
+  float acc = 0.0f;
+  int32_t ccount = 0; // matches so far in this lane's class (same value in all lanes of a class)
+  for (int32_t base = 0; base < dv; base += kChunk) {
+    int32_t x[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int32_t p = base + lane + 32 * j;
+      x[j] = p < dv ? __ldg(col + vs + p) : kEmpty;
+    }
+    bool f[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) f[j] = x[j] != kEmpty && probe(x[j]);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const unsigned mb = __ballot_sync(kFull, x[j] == u && x[j] != kEmpty);
+      if (mb) mirror = (mirror == -1 && __popc(mb) == 1) ? base + 32 * j + __ffs(mb) - 1 : -2;
+    }
+    if (!kWeighted) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) cnt += __popc(__ballot_sync(kFull, f[j]));
+    } else {
+      // position base + lane + 32j has class (lane & 7); within a class, ascending positions
+      // are j-major, lane-minor: exactly the order of these ballots.
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const unsigned m = __ballot_sync(kFull, f[j]);
+        const float val = f[j] ? __ldg(w + x[j]) : 0.0f;
+        acc = warp_ordered_fold(m & kClass0, val, acc);
+        if (f[j] && my_class != 0) cls.put(my_class, ccount + __popc(m & my_cmask & lt), val);
+        ccount += __popc(m & my_cmask);
+      }
+    }
+  }
+  if (!kWeighted) return (float)cnt;
+  __syncwarp();
+  bool overflow = false;
+  for (int c = 1; c < 8; ++c) overflow |= __shfl_sync(kFull, ccount, c) > cls.cap;
+  if (overflow) return task_strided<true>(probe, col, w, u, vs, dv, mirror);
+  for (int c = 1; c < 8; ++c) {
+    const int32_t nc = __shfl_sync(kFull, ccount, c);
+    for (int32_t t = 0; t < nc; t += 32) {
+      const int32_t k = nc - t < 32 ? nc - t : 32;
+      const float v = lane < k ? cls.get(c, t + lane) : 0.0f;
+      for (int b = 0; b < k; ++b) acc = __shfl_sync(kFull, v, b) + acc;
+    }
+  }
+  __syncwarp();
+  return acc;
+}
+
+// J for a task and the directed edges it serves (see the header comment).
 template <bool kEC, bool kWeighted>
 __device__ __forceinline__ void write_task(float I, int32_t du, int32_t dv, float Su, float Sv,
                                            int64_t e_uv, int64_t e_vu, float *__restrict__ out) {
   float J;
   if (kEC) {
-    J = I / ((float)(dv + du) - I); // jaccard.cpp:741, Ni = d_v (csrInd[tid]), Nj = d_u
+    J = I / ((float)(dv + du) - I); // jaccard.cpp:741 with Ni = d_v (csrInd[tid]), Nj = d_u
   } else {
     const float Ws = kWeighted ? (Su + Sv) : ((float)du + (float)dv); // jaccard.cpp:258,339
     const float Wu = Ws - I;                                           // jaccard.cpp:617
@@ -150,135 +244,363 @@ __device__ __forceinline__ void write_task(float I, int32_t du, int32_t dv, floa
   }
 }
 
-// ---------------------------------------------------------------- plan: bin the rows
-__global__ void plan_kernel(int32_t n, const int32_t *__restrict__ row_ptr, int32_t *__restrict__ rows,
-                            int32_t *__restrict__ cnt) {
-  // rows: four regions of n entries (row lists per bin)
-  for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n;
-       u += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t d = __ldg(row_ptr + u + 1) - __ldg(row_ptr + u);
-    if (d == 0) continue;
-    const int b = d <= kB0Max ? 0 : (d <= kB1Max ? 1 : (d <= kB2Max ? 2 : 3));
-    const int32_t slot = atomicAdd(cnt + kCntBin0 + b, 1);
-    rows[(int64_t)b * n + slot] = (int32_t)u;
+// ---------------------------------------------------------------- plan: degree-sorted rows
+// Sort key = bin * 32 + (31 - ceil(log2 d)): hubs, then B2, B1, B0, each largest first.
+__device__ __forceinline__ int plan_key(int32_t d) {
+  const int bin = d > kB2Max ? 0 : (d > kB1Max ? 1 : (d > kB0Max ? 2 : 3));
+  const int lg = d <= 1 ? 0 : 32 - __clz(d - 1);
+  return bin * 32 + (31 - lg);
+}
+
+template <bool kScatter>
+__global__ void plan_kernel(int32_t n, const int32_t *__restrict__ row_ptr, int32_t *__restrict__ cnt,
+                            int32_t *__restrict__ rows) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t u = base + threadIdx.x;
+    int key = -1;
+    if (u < n) {
+      const int32_t d = __ldg(row_ptr + u + 1) - __ldg(row_ptr + u);
+      if (d > 0) key = plan_key(d);
+    }
+    const unsigned peers = __match_any_sync(kFull, key);
+    if (key >= 0) {
+      const int leader = __ffs(peers) - 1;
+      int32_t b = 0;
+      if (lane == leader) b = atomicAdd(cnt + kCntKeys + key, __popc(peers));
+      b = __shfl_sync(peers, b, leader);
+      if (kScatter) rows[cnt[kOffKeys + key] + b + __popc(peers & ((1u << lane) - 1u))] = (int32_t)u;
+    }
   }
 }
 
+// Exclusive scan of the key counts; resets the counts to serve as scatter cursors.
+__global__ void plan_offsets_kernel(int32_t *__restrict__ cnt) {
+  __shared__ int32_t s[kKeys];
+  const int t = threadIdx.x;
+  s[t] = cnt[kCntKeys + t];
+  __syncthreads();
+  if (t == 0) {
+    int32_t run = 0;
+    for (int k = 0; k < kKeys; ++k) {
+      cnt[kOffKeys + k] = run;
+      run += s[k];
+    }
+    cnt[kOffKeys + kKeys] = run;
+  }
+  cnt[kCntKeys + t] = 0;
+}
+
+// Hub work units: a hub row with d tasks gives ceil(d / kHubTasksPerUnit) units.
+__global__ void hub_units_kernel(const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ rows,
+                                 int32_t *__restrict__ cnt, int32_t *__restrict__ unit_off) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int32_t h0 = cnt[kOffKeys + 0], h1 = cnt[kOffKeys + 32];
+  int32_t run = 0;
+  for (int32_t i = h0; i < h1; ++i) {
+    unit_off[i - h0] = run;
+    const int32_t u = rows[i];
+    const int32_t d = row_ptr[u + 1] - row_ptr[u];
+    run += (d + kHubTasksPerUnit - 1) / kHubTasksPerUnit;
+  }
+  unit_off[h1 - h0] = run;
+  cnt[kNumHubUnits] = run;
+}
+
 __global__ void fill_bits_kernel(int64_t n, uint32_t *__restrict__ x, uint32_t bits) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+  const int64_t n4 = (reinterpret_cast<uintptr_t>(x) & 15u) ? 0 : n >> 2; // vector stores need 16 B alignment
+  uint4 *x4 = reinterpret_cast<uint4 *>(x);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x)
+    x4[i] = make_uint4(bits, bits, bits, bits);
+  for (int64_t i = (n4 << 2) + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     x[i] = bits;
 }
 
-// ---------------------------------------------------------------- B0/B1: one warp per row
-template <bool kEC, bool kWeighted, int kSlots>
-__global__ void __launch_bounds__(kRowThreads) warp_rows_kernel(
-    int32_t n, const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
-    const float *__restrict__ w, const float *__restrict__ S, const int32_t *__restrict__ rows,
-    const int32_t *__restrict__ count, float *__restrict__ out) {
-  __shared__ int32_t tables[kRowThreads / 32][kSlots];
+// ---------------------------------------------------------------- B0: lane per task
+template <bool kEC, bool kWeighted>
+__global__ void __launch_bounds__(kRowThreads) b0_kernel(
+    const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
+    const float *__restrict__ S, const int32_t *__restrict__ rows, const int32_t *__restrict__ cnt,
+    float *__restrict__ out) {
+  __shared__ int32_t tables[kRowThreads / 32][kB0Slots];
   const int lane = threadIdx.x & 31;
   int32_t *t = tables[threadIdx.x >> 5];
-  const int32_t nrows = *count;
+  const int32_t r0 = cnt[kOffKeys + 96], r1 = cnt[kOffKeys + 128];
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nrows; i += nwarps) {
+  for (int64_t i = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < r1; i += nwarps) {
     const int32_t u = rows[i];
     const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
-    uint32_t size = 2u * (uint32_t)du;
-    size = size < 32u ? 32u : size;
+    const uint32_t size = 2u * kB0Max;
+    t[lane] = kEmpty;
+    t[lane + 32] = kEmpty;
+    __syncwarp();
+    if (lane < du) hset_insert(t, size, __ldg(col + us + lane));
+    __syncwarp();
+    if (lane < du) {
+      const HashProbe probe{t, size};
+      const int32_t v = __ldg(col + us + lane);
+      const int32_t vs = __ldg(row_ptr + v), dv = __ldg(row_ptr + v + 1) - vs;
+      if (dv <= du) {
+        int32_t mirror = -1;
+        float I;
+        if (!kWeighted) {
+          int32_t c = 0;
+          for (int32_t p = 0; p < dv; ++p) {
+            const int32_t x = __ldg(col + vs + p);
+            c += probe(x);
+            if (x == u) mirror = mirror == -1 ? p : -2;
+          }
+          I = (float)c;
+        } else {
+          float acc = 0.0f;
+          for (int il = 0; il < kIsILanes; ++il)
+            for (int32_t p = il; p < dv; p += kIsILanes) {
+              const int32_t x = __ldg(col + vs + p);
+              if (probe(x)) acc = __ldg(w + x) + acc;
+              if (x == u) mirror = mirror == -1 ? p : -2;
+            }
+          I = acc;
+        }
+        write_task<kEC, kWeighted>(I, du, dv, kWeighted ? __ldg(S + u) : 0.0f,
+                                   kWeighted ? __ldg(S + v) : 0.0f, (int64_t)us + lane,
+                                   mirror >= 0 ? (int64_t)vs + mirror : -1, out);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------- B1: warp per row
+template <bool kEC, bool kWeighted>
+__global__ void __launch_bounds__(kRowThreads) b1_kernel(
+    const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
+    const float *__restrict__ S, const int32_t *__restrict__ rows, const int32_t *__restrict__ cnt,
+    float *__restrict__ out) {
+  __shared__ int32_t tables[kRowThreads / 32][kB1Slots];
+  __shared__ float streams[kWeighted ? kRowThreads / 32 : 1][kWeighted ? 7 * kB1Cap : 1];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int32_t *t = tables[wid];
+  const SmemClassStreams cls{streams[kWeighted ? wid : 0], kB1Cap};
+  const int32_t r0 = cnt[kOffKeys + 64], r1 = cnt[kOffKeys + 96];
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t i = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < r1; i += nwarps) {
+    const int32_t u = rows[i];
+    const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
+    const uint32_t size = 2u * (uint32_t)du;
     for (uint32_t k = lane; k < size; k += 32) t[k] = kEmpty;
     __syncwarp();
     for (int32_t k = lane; k < du; k += 32) hset_insert(t, size, __ldg(col + us + k));
     __syncwarp();
-    const float Su = kWeighted ? __ldg(S + u) : 0.0f;
     const HashProbe probe{t, size};
-    for (int32_t k = 0; k < du; ++k) {
-      const int32_t v = __ldg(col + us + k);
-      const int32_t vs = __ldg(row_ptr + v), dv = __ldg(row_ptr + v + 1) - vs;
-      if (dv > du) continue;
-      int32_t mirror;
-      const float I = warp_task<kWeighted>(probe, col, w, u, vs, dv, mirror);
-      if (lane == 0)
-        write_task<kEC, kWeighted>(I, du, dv, Su, kWeighted ? __ldg(S + v) : 0.0f, (int64_t)us + k,
-                                   mirror >= 0 ? (int64_t)vs + mirror : -1, out);
+    const float Su = kWeighted ? __ldg(S + u) : 0.0f;
+    for (int32_t k0 = 0; k0 < du; k0 += 32) {
+      // lanes fetch 32 candidate tasks at once; the warp then runs them one by one
+      int32_t v = -1, vs = 0, dv = 0;
+      if (k0 + lane < du) {
+        v = __ldg(col + us + k0 + lane);
+        vs = __ldg(row_ptr + v);
+        dv = __ldg(row_ptr + v + 1) - vs;
+      }
+      unsigned todo = __ballot_sync(kFull, v >= 0 && dv <= du);
+      while (todo) {
+        const int b = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int32_t tv = __shfl_sync(kFull, v, b), tvs = __shfl_sync(kFull, vs, b),
+                      tdv = __shfl_sync(kFull, dv, b);
+        int32_t mirror;
+        const float I = task_stream<kWeighted>(probe, col, w, u, tvs, tdv, mirror, cls);
+        if (lane == 0)
+          write_task<kEC, kWeighted>(I, du, tdv, Su, kWeighted ? __ldg(S + tv) : 0.0f, (int64_t)us + k0 + b,
+                                     mirror >= 0 ? (int64_t)tvs + mirror : -1, out);
+      }
     }
     __syncwarp();
   }
 }
 
-// ---------------------------------------------------------------- B2/B3: one CTA per row
-template <bool kEC, bool kWeighted, bool kHub>
-__global__ void __launch_bounds__(kB2Threads) cta_rows_kernel(
-    int32_t n, const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
-    const float *__restrict__ w, const float *__restrict__ S, const int32_t *__restrict__ rows,
-    const int32_t *__restrict__ count, int32_t *__restrict__ work_ctr, float *__restrict__ out) {
+// ---------------------------------------------------------------- B2: CTA per row
+template <bool kEC, bool kWeighted>
+__global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
+    const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
+    const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
+    float *__restrict__ out, float *__restrict__ scratch) {
   extern __shared__ int32_t table[];
-  __shared__ int32_t s_row;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int32_t nrows = *count;
+  __shared__ int32_t s_row, s_task;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kB2Threads / 32) + wid) * 7 * kCap, kCap};
+  const int32_t r0 = cnt[kOffKeys + 32], r1 = cnt[kOffKeys + 64];
   for (;;) {
-    if (threadIdx.x == 0) s_row = atomicAdd(work_ctr, 1);
+    if (threadIdx.x == 0) {
+      s_row = r0 + atomicAdd(cnt + kCtrB2, 1);
+      s_task = 0;
+    }
     __syncthreads();
     const int32_t i = s_row;
-    __syncthreads();
-    if (i >= nrows) break;
+    if (i >= r1) break;
     const int32_t u = rows[i];
     const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
-    const uint32_t size = 2u * (uint32_t)du;
-    if (!kHub) {
-      for (uint32_t k = threadIdx.x; k < size; k += blockDim.x) table[k] = kEmpty;
-      __syncthreads();
-      for (int32_t k = threadIdx.x; k < du; k += blockDim.x) hset_insert(table, size, __ldg(col + us + k));
-      __syncthreads();
-    }
+    uint32_t size = 4u * (uint32_t)du;
+    size = size > (uint32_t)kB2Slots ? (uint32_t)kB2Slots : size;
+    for (uint32_t k = threadIdx.x; k < size; k += blockDim.x) table[k] = kEmpty;
+    __syncthreads();
+    for (int32_t k = threadIdx.x; k < du; k += blockDim.x) hset_insert(table, size, __ldg(col + us + k));
+    __syncthreads();
+    const HashProbe probe{table, size};
     const float Su = kWeighted ? __ldg(S + u) : 0.0f;
-    for (int32_t k = warp; k < du; k += nw) {
-      const int32_t v = __ldg(col + us + k);
-      const int32_t vs = __ldg(row_ptr + v), dv = __ldg(row_ptr + v + 1) - vs;
-      if (dv > du) continue;
-      int32_t mirror;
-      float I;
-      if (kHub)
-        I = warp_task<kWeighted>(SearchProbe{col, us, us + du - 1}, col, w, u, vs, dv, mirror);
-      else
-        I = warp_task<kWeighted>(HashProbe{table, size}, col, w, u, vs, dv, mirror);
-      if (lane == 0)
-        write_task<kEC, kWeighted>(I, du, dv, Su, kWeighted ? __ldg(S + v) : 0.0f, (int64_t)us + k,
-                                   mirror >= 0 ? (int64_t)vs + mirror : -1, out);
+    for (;;) {
+      int32_t k0 = 0;
+      if (lane == 0) k0 = atomicAdd(&s_task, 32);
+      k0 = __shfl_sync(kFull, k0, 0);
+      if (k0 >= du) break;
+      int32_t v = -1, vs = 0, dv = 0;
+      if (k0 + lane < du) {
+        v = __ldg(col + us + k0 + lane);
+        vs = __ldg(row_ptr + v);
+        dv = __ldg(row_ptr + v + 1) - vs;
+      }
+      unsigned todo = __ballot_sync(kFull, v >= 0 && dv <= du);
+      while (todo) {
+        const int b = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int32_t tv = __shfl_sync(kFull, v, b), tvs = __shfl_sync(kFull, vs, b),
+                      tdv = __shfl_sync(kFull, dv, b);
+        int32_t mirror;
+        const float I = task_stream<kWeighted>(probe, col, w, u, tvs, tdv, mirror, cls);
+        if (lane == 0)
+          write_task<kEC, kWeighted>(I, du, tdv, Su, kWeighted ? __ldg(S + tv) : 0.0f, (int64_t)us + k0 + b,
+                                     mirror >= 0 ? (int64_t)tvs + mirror : -1, out);
+      }
     }
     __syncthreads();
   }
 }
 
-// ---------------------------------------------------------------- fix-up of uncovered edges
-// Any edge still holding the sentinel is computed on its own, with the reference's own
-// ref/cur choice (VC jaccard.cpp:333-336, EC jaccard.cpp:716-719) and binary search.
+// ---------------------------------------------------------------- hubs: 8-CTA clusters
+// A cluster takes one hub unit (hub row u, task range) at a time: its CTAs build N(u) as a
+// bitmap over [0, n) in the cluster's own global slot, all warps stream the unit's tasks
+// against it (L2 hits), then the bits are cleared again.  Cluster barriers separate the
+// phases; the unit index and task counter live in rank 0's shared memory.
 template <bool kEC, bool kWeighted>
-__global__ void __launch_bounds__(256) fixup_kernel(int32_t n, const int32_t *__restrict__ row_ptr,
+__global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
+    const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
+    const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
+    const int32_t *__restrict__ unit_off, uint32_t *__restrict__ bitmaps, int64_t words,
+    float *__restrict__ out, float *__restrict__ scratch) {
+  cg::cluster_group cluster = cg::this_cluster();
+  __shared__ int32_t s_unit, s_task;
+  const unsigned rank = cluster.block_rank();
+  const int64_t cid = blockIdx.x / kCluster;
+  uint32_t *bm = bitmaps + cid * words;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kHubThreads / 32) + wid) * 7 * kCap, kCap};
+  int32_t *unit_p = cluster.map_shared_rank(&s_unit, 0);
+  int32_t *task_p = cluster.map_shared_rank(&s_task, 0);
+  const int32_t h0 = cnt[kOffKeys + 0];
+  const int32_t nunits = cnt[kNumHubUnits];
+  const int32_t nhubs = cnt[kOffKeys + 32] - h0;
+  if (rank == 0 && threadIdx.x == 0) {
+    s_unit = atomicAdd(cnt + kCtrHub, 1);
+    s_task = 0;
+  }
+  cluster.sync();
+  for (;;) {
+    const int32_t unit = *unit_p;
+    if (unit >= nunits) break;
+    // locate the hub of this unit
+    int32_t lo = 0, hi = nhubs - 1;
+    while (lo < hi) {
+      const int32_t mid = (lo + hi + 1) >> 1;
+      if (unit_off[mid] <= unit) lo = mid; else hi = mid - 1;
+    }
+    const int32_t u = rows[h0 + lo];
+    const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
+    const int32_t k_begin = (unit - unit_off[lo]) * kHubTasksPerUnit;
+    const int32_t k_end = min(du, k_begin + kHubTasksPerUnit);
+    for (int32_t k = rank * blockDim.x + threadIdx.x; k < du; k += kCluster * blockDim.x) {
+      const int32_t x = __ldg(col + us + k);
+      atomicOr(bm + (x >> 5), 1u << (x & 31));
+    }
+    cluster.sync();
+    const BitmapProbe probe{bm};
+    const float Su = kWeighted ? __ldg(S + u) : 0.0f;
+    for (;;) {
+      int32_t k0 = 0;
+      if (lane == 0) k0 = k_begin + atomicAdd(task_p, 32);
+      k0 = __shfl_sync(kFull, k0, 0);
+      if (k0 >= k_end) break;
+      int32_t v = -1, vs = 0, dv = 0;
+      if (k0 + lane < k_end) {
+        v = __ldg(col + us + k0 + lane);
+        vs = __ldg(row_ptr + v);
+        dv = __ldg(row_ptr + v + 1) - vs;
+      }
+      unsigned todo = __ballot_sync(kFull, v >= 0 && dv <= du);
+      while (todo) {
+        const int b = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int32_t tv = __shfl_sync(kFull, v, b), tvs = __shfl_sync(kFull, vs, b),
+                      tdv = __shfl_sync(kFull, dv, b);
+        int32_t mirror;
+        const float I = task_stream<kWeighted>(probe, col, w, u, tvs, tdv, mirror, cls);
+        if (lane == 0)
+          write_task<kEC, kWeighted>(I, du, tdv, Su, kWeighted ? __ldg(S + tv) : 0.0f, (int64_t)us + k0 + b,
+                                     mirror >= 0 ? (int64_t)tvs + mirror : -1, out);
+      }
+    }
+    cluster.sync();
+    for (int32_t k = rank * blockDim.x + threadIdx.x; k < du; k += kCluster * blockDim.x)
+      __stcg(bm + (__ldg(col + us + k) >> 5), 0u);
+    if (rank == 0 && threadIdx.x == 0) {
+      s_unit = atomicAdd(cnt + kCtrHub, 1);
+      s_task = 0;
+    }
+    cluster.sync();
+  }
+  // no CTA may exit while another can still read rank 0's shared memory
+  cluster.sync();
+}
+
+// ---------------------------------------------------------------- fix-up of uncovered edges
+// Any edge still holding the sentinel is computed on its own with the reference's ref/cur
+// choice (VC jaccard.cpp:333-336, EC jaccard.cpp:716-719) and binary search.
+template <bool kEC, bool kWeighted>
+__global__ void __launch_bounds__(256) fixup_kernel(int32_t n, int64_t e, const int32_t *__restrict__ row_ptr,
                                                     const int32_t *__restrict__ col,
                                                     const float *__restrict__ w,
                                                     const float *__restrict__ S,
                                                     float *__restrict__ out) {
   const int lane = threadIdx.x & 31;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  uint32_t *outb = reinterpret_cast<uint32_t *>(out);
-  for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += nwarps) {
-    const int32_t us = __ldg(row_ptr + u), ue = __ldg(row_ptr + u + 1), du = ue - us;
-    for (int32_t j0 = us; j0 < ue; j0 += 32) {
-      const int32_t j = j0 + lane;
-      unsigned todo = __ballot_sync(kFull, j < ue && outb[j] == kUnwritten);
+  const uint32_t *outb = reinterpret_cast<const uint32_t *>(out);
+  for (int64_t j0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 128; j0 < e; j0 += nwarps * 128) {
+    uint32_t b[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int64_t j = j0 + lane + 32 * q;
+      b[q] = j < e ? outb[j] : 0u;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      unsigned todo = __ballot_sync(kFull, b[q] == kUnwritten);
       while (todo) {
-        const int32_t jj = j0 + __ffs(todo) - 1;
+        const int64_t jj = j0 + 32 * q + __ffs(todo) - 1;
         todo &= todo - 1;
+        // source row: the last u with row_ptr[u] <= jj
+        int32_t lo = 0, hi = n - 1;
+        while (lo < hi) {
+          const int32_t mid = (lo + hi + 1) >> 1;
+          if (__ldg(row_ptr + mid) <= jj) lo = mid; else hi = mid - 1;
+        }
+        const int32_t u = lo;
+        const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
         const int32_t v = __ldg(col + jj);
         const int32_t vs = __ldg(row_ptr + v), dv = __ldg(row_ptr + v + 1) - vs;
-        // ref/cur per the reference rule for this directed edge
         const bool u_is_ref = kEC ? !(dv < du) : (du < dv);
         const int32_t rs = u_is_ref ? us : vs, rl = u_is_ref ? du : dv;
         const int32_t cs = u_is_ref ? vs : us, cl = u_is_ref ? dv : du;
         int32_t dummy;
-        const float I = warp_task<kWeighted && !kEC>(SearchProbe{col, cs, cs + cl - 1}, col, w,
-                                                      -1, rs, rl, dummy);
+        const float I = task_strided<kWeighted && !kEC>(SearchProbe{col, cs, cs + cl - 1}, col, w, -1, rs, rl, dummy);
         if (lane == 0) {
           float J;
           if (kEC) {
@@ -295,52 +617,104 @@ __global__ void __launch_bounds__(256) fixup_kernel(int32_t n, const int32_t *__
 }
 
 // ---------------------------------------------------------------- host driver
-size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-size_t workspace_bytes(int32_t n, bool weighted_vc) {
-  return align256(sizeof(int32_t) * kCounters) + align256(sizeof(int32_t) * (size_t)n * kBins) +
-         (weighted_vc ? align256(sizeof(float) * (size_t)n) : 0);
+struct Layout {
+  size_t cnt, rows, unit_off, S, scratch, bitmaps, total;
+  int64_t words;
+  int clusters;
+};
+
+static Layout layout(int32_t n, int32_t e, bool weighted_vc) {
+  Layout L;
+  const int sms = sm_count();
+  L.clusters = sms / kCluster > 0 ? sms / kCluster : 1;
+  L.words = ((int64_t)n + 31) / 32;
+  size_t off = 0;
+  L.cnt = off;      off += align256(sizeof(int32_t) * kCounters);
+  L.rows = off;     off += align256(sizeof(int32_t) * (size_t)n);
+  // every hub row holds more than kB2Max edges
+  const size_t max_hubs = std::min<size_t>((size_t)n, (size_t)e / (kB2Max + 1));
+  L.unit_off = off; off += align256(sizeof(int32_t) * (max_hubs + 2));
+  L.S = off;        off += weighted_vc ? align256(sizeof(float) * (size_t)n) : 0;
+  // class streams: one region per warp of the B2 grid (sms CTAs) or the hub grid
+  const size_t warps = (size_t)(sms > L.clusters * kCluster ? sms : L.clusters * kCluster) * 32;
+  L.scratch = off;  off += weighted_vc ? align256(sizeof(float) * warps * 7 * kCap) : 0;
+  L.bitmaps = off;  off += align256(sizeof(uint32_t) * (size_t)L.words * L.clusters);
+  L.total = off;
+  return L;
 }
 
 template <bool kEC, bool kWeighted>
-jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws, cudaStream_t s) {
+static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws, cudaStream_t s) {
   const int32_t n = g.n;
-  int32_t *cnt = reinterpret_cast<int32_t *>(ws);
-  int32_t *rows = reinterpret_cast<int32_t *>(ws + align256(sizeof(int32_t) * kCounters));
-  float *S = kWeighted ? reinterpret_cast<float *>(ws + align256(sizeof(int32_t) * kCounters) +
-                                                   align256(sizeof(int32_t) * (size_t)n * kBins))
-                       : nullptr;
+  const Layout L = layout(n, g.e, kWeighted);
+  int32_t *cnt = reinterpret_cast<int32_t *>(ws + L.cnt);
+  int32_t *rows = reinterpret_cast<int32_t *>(ws + L.rows);
+  int32_t *unit_off = reinterpret_cast<int32_t *>(ws + L.unit_off);
+  float *S = kWeighted ? reinterpret_cast<float *>(ws + L.S) : nullptr;
+  float *scratch = kWeighted ? reinterpret_cast<float *>(ws + L.scratch) : nullptr;
+  uint32_t *bitmaps = reinterpret_cast<uint32_t *>(ws + L.bitmaps);
   const int sms = sm_count();
-  cudaError_t ce = cudaMemsetAsync(cnt, 0, sizeof(int32_t) * kCounters, s);
-  if (ce != cudaSuccess) return set_cuda_error(ce);
   jx_status st;
-  plan_kernel<<<sms * 8, 256, 0, s>>>(n, g.row_ptr, rows, cnt);
+  cudaError_t ce;
+  prof_mark("start", s);
+  if ((ce = cudaMemsetAsync(cnt, 0, sizeof(int32_t) * kCounters, s)) != cudaSuccess) return set_cuda_error(ce);
+  if ((ce = cudaMemsetAsync(bitmaps, 0, sizeof(uint32_t) * (size_t)L.words * L.clusters, s)) != cudaSuccess)
+    return set_cuda_error(ce);
+  plan_kernel<false><<<sms * 4, 256, 0, s>>>(n, g.row_ptr, cnt, rows);
   if ((st = check_launch()) != JX_OK) return st;
+  plan_offsets_kernel<<<1, kKeys, 0, s>>>(cnt);
+  if ((st = check_launch()) != JX_OK) return st;
+  plan_kernel<true><<<sms * 4, 256, 0, s>>>(n, g.row_ptr, cnt, rows);
+  if ((st = check_launch()) != JX_OK) return st;
+  hub_units_kernel<<<1, 32, 0, s>>>(g.row_ptr, rows, cnt, unit_off);
+  if ((st = check_launch()) != JX_OK) return st;
+  prof_mark("plan", s);
   if (kWeighted) {
     if ((st = jx_rowsum(n, g.e, g.row_ptr, g.col_idx, w, S, (jx_stream_t)s)) != JX_OK) return st;
+    prof_mark("rowsum", s);
   }
-  fill_bits_kernel<<<sms * 8, 256, 0, s>>>(g.e, reinterpret_cast<uint32_t *>(out), kUnwritten);
+  fill_bits_kernel<<<sms * 4, 256, 0, s>>>(g.e, reinterpret_cast<uint32_t *>(out), kUnwritten);
   if ((st = check_launch()) != JX_OK) return st;
+  prof_mark("sentinel_fill", s);
 
-  const size_t smem_b2 = sizeof(int32_t) * 2 * (size_t)kB2Max;
-  ce = cudaFuncSetAttribute(cta_rows_kernel<kEC, kWeighted, false>,
-                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b2);
+  {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(L.clusters * kCluster);
+    cfg.blockDim = dim3(kHubThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kCluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    ce = cudaLaunchKernelEx(&cfg, hub_kernel<kEC, kWeighted>, (const int32_t *)g.row_ptr,
+                            (const int32_t *)g.col_idx, w, (const float *)S, (const int32_t *)rows, cnt,
+                            (const int32_t *)unit_off, bitmaps, (int64_t)L.words, out, scratch);
+    if (ce != cudaSuccess) return set_cuda_error(ce);
+    if ((st = check_launch()) != JX_OK) return st;
+    prof_mark("hub_rows", s);
+  }
+  const size_t smem_b2 = sizeof(int32_t) * (size_t)kB2Slots;
+  ce = cudaFuncSetAttribute(b2_kernel<kEC, kWeighted>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b2);
   if (ce != cudaSuccess) return set_cuda_error(ce);
-  // hubs first (longest rows), then the CTA bin, then the warp bins
-  cta_rows_kernel<kEC, kWeighted, true><<<sms, kB2Threads, 0, s>>>(
-      n, g.row_ptr, g.col_idx, w, S, rows + 3 * (size_t)n, cnt + kCntBin0 + 3, cnt + kWorkBin3, out);
+  b2_kernel<kEC, kWeighted><<<sms, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out, scratch);
   if ((st = check_launch()) != JX_OK) return st;
-  cta_rows_kernel<kEC, kWeighted, false><<<sms, kB2Threads, smem_b2, s>>>(
-      n, g.row_ptr, g.col_idx, w, S, rows + 2 * (size_t)n, cnt + kCntBin0 + 2, cnt + kWorkBin2, out);
+  prof_mark("cta_rows", s);
+  b1_kernel<kEC, kWeighted><<<sms * 4, kRowThreads, 0, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
   if ((st = check_launch()) != JX_OK) return st;
-  warp_rows_kernel<kEC, kWeighted, kB1Slots><<<sms * 4, kRowThreads, 0, s>>>(
-      n, g.row_ptr, g.col_idx, w, S, rows + 1 * (size_t)n, cnt + kCntBin0 + 1, out);
+  prof_mark("warp_rows", s);
+  b0_kernel<kEC, kWeighted><<<sms * 8, kRowThreads, 0, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
   if ((st = check_launch()) != JX_OK) return st;
-  warp_rows_kernel<kEC, kWeighted, kB0Slots><<<sms * 8, kRowThreads, 0, s>>>(
-      n, g.row_ptr, g.col_idx, w, S, rows, cnt + kCntBin0, out);
+  prof_mark("lane_rows", s);
+  fixup_kernel<kEC, kWeighted><<<sms * 8, 256, 0, s>>>(n, g.e, g.row_ptr, g.col_idx, w, S, out);
   if ((st = check_launch()) != JX_OK) return st;
-  fixup_kernel<kEC, kWeighted><<<sms * 8, 256, 0, s>>>(n, g.row_ptr, g.col_idx, w, S, out);
-  return check_launch();
+  prof_mark("fixup", s);
+  return JX_OK;
 }
 
 } // namespace jx
@@ -351,18 +725,18 @@ extern "C" {
 
 size_t jx_jaccard_workspace_size(const jx_csr *g, int weighted, jx_algo algo) {
   if (!g || g->n < 0) return 0;
-  return workspace_bytes(g->n, weighted && algo == JX_ALGO_VERTEX_CENTRIC);
+  return layout(g->n, g->e, weighted && algo == JX_ALGO_VERTEX_CENTRIC).total;
 }
 
 jx_status jx_jaccard_ws(const jx_csr *g, const float *vertex_w, float *out_j, jx_algo algo,
-                        void *workspace, size_t workspace_bytes_, jx_stream_t stream) {
+                        void *workspace, size_t workspace_bytes, jx_stream_t stream) {
   if (!g || g->n < 0 || g->e < 0) return JX_ERR_INVALID;
   if (algo != JX_ALGO_VERTEX_CENTRIC && algo != JX_ALGO_EDGE_CENTRIC) return JX_ERR_INVALID;
   if (g->n == 0 || g->e == 0) return JX_OK;
   if (!g->row_ptr || !g->col_idx || !out_j) return JX_ERR_INVALID;
   const bool ec = algo == JX_ALGO_EDGE_CENTRIC;
   const bool weighted = vertex_w != nullptr && !ec; // EC ignores weights (jaccard.cpp:790)
-  if (!workspace || workspace_bytes_ < workspace_bytes(g->n, weighted) ||
+  if (!workspace || workspace_bytes < layout(g->n, g->e, weighted).total ||
       (reinterpret_cast<uintptr_t>(workspace) & 255u))
     return JX_ERR_INVALID;
   char *ws = static_cast<char *>(workspace);
@@ -380,7 +754,7 @@ jx_status jx_jaccard(const jx_csr *g, const float *vertex_w, float *out_j, jx_al
   cudaStream_t s = (cudaStream_t)stream;
   void *ws = nullptr;
   cudaError_t ce = cudaMallocAsync(&ws, bytes, s);
-  if (ce != cudaSuccess) return ce == cudaErrorMemoryAllocation ? JX_ERR_NOMEM : set_cuda_error(ce);
+  if (ce != cudaSuccess) return set_cuda_error(ce);
   const jx_status st = jx_jaccard_ws(g, vertex_w, out_j, algo, ws, bytes, stream);
   ce = cudaFreeAsync(ws, s);
   if (st != JX_OK) return st;

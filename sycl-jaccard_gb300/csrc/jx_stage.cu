@@ -7,31 +7,51 @@ namespace jx {
 
 // ---------------------------------------------------------------- RowSum
 // Jaccard_RowSumKernel (jaccard.cpp:236-261) + parallel_prefix_sum (jaccard.cpp:53-137).
-// One warp per row.  Each 32-element chunk is reduced with the scan's tree (lanes past the
-// row end hold 0.0, jaccard.cpp:98), then the carry (the previous chunk's total) is added:
+// Each 32-element chunk is reduced with the scan's tree (lanes past the row end hold 0.0,
+// jaccard.cpp:98), then the carry (the previous chunk's total) is added:
 // T = tree(chunk) + T_prev (jaccard.cpp:119).  The row total is lane 31's final value.
+// A row of at most 32 elements is one chunk: one thread evaluates the 32-leaf tree itself
+// (pairs (2i+1, 2i), then pairs of pairs, ...; zeros past the end), which is the same set of
+// additions the scan performs for lane 31.  Longer rows are taken by the whole warp.
 template <bool kWeighted>
 __global__ void __launch_bounds__(256) rowsum_kernel(int32_t n, const int32_t *__restrict__ row_ptr,
                                                       const int32_t *__restrict__ ind,
                                                       const float *__restrict__ w,
                                                       float *__restrict__ work) {
   const int lane = threadIdx.x & 31;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  if (!kWeighted) {
-    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
-         r += (int64_t)gridDim.x * blockDim.x)
-      work[r] = (float)(__ldg(row_ptr + r + 1) - __ldg(row_ptr + r));
-    return;
-  }
-  for (int64_t r = warp; r < n; r += nwarps) {
-    const int32_t start = __ldg(row_ptr + r), len = __ldg(row_ptr + r + 1) - start;
-    float total = 0.0f;
-    for (int32_t i0 = 0; i0 < len; i0 += 32) {
-      const float x = (i0 + lane < len) ? __ldg(w + __ldg(ind + start + i0 + lane)) : 0.0f;
-      total = warp_tree_sum(x) + total;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = base + threadIdx.x;
+    int32_t start = 0, len = 0;
+    if (r < n) {
+      start = __ldg(row_ptr + r);
+      len = __ldg(row_ptr + r + 1) - start;
     }
-    if (lane == 0) work[r] = total;
+    if (!kWeighted) {
+      if (r < n) work[r] = (float)len;
+      continue;
+    }
+    if (r < n && len <= 32) {
+      float x[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) x[i] = i < len ? __ldg(w + __ldg(ind + start + i)) : 0.0f;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1)
+#pragma unroll
+        for (int i = 0; i < 32; i += 2 * o) x[i] = x[i + o] + x[i];
+      work[r] = x[0] + 0.0f;
+    }
+    unsigned longs = __ballot_sync(kFull, r < n && len > 32);
+    while (longs) {
+      const int b = __ffs(longs) - 1;
+      longs &= longs - 1;
+      const int32_t s0 = __shfl_sync(kFull, start, b), l0 = __shfl_sync(kFull, len, b);
+      float total = 0.0f;
+      for (int32_t i0 = 0; i0 < l0; i0 += 32) {
+        const float x = (i0 + lane < l0) ? __ldg(w + __ldg(ind + s0 + i0 + lane)) : 0.0f;
+        total = warp_tree_sum(x) + total;
+      }
+      if (lane == b) work[r] = total;
+    }
   }
 }
 
@@ -173,7 +193,7 @@ jx_status jx_rowsum(int32_t n, int32_t e, const int32_t *row_ptr, const int32_t 
   if (n == 0) return JX_OK;
   cudaStream_t s = (cudaStream_t)stream;
   if (w)
-    rowsum_kernel<true><<<grid_for((int64_t)n * 32, 256), 256, 0, s>>>(n, row_ptr, ind, w, work);
+    rowsum_kernel<true><<<grid_for(n, 256), 256, 0, s>>>(n, row_ptr, ind, w, work);
   else
     rowsum_kernel<false><<<grid_for(n, 256), 256, 0, s>>>(n, row_ptr, ind, w, work);
   return check_launch();
