@@ -255,6 +255,8 @@ def run_gpu(args, world, rank, local):
     torch.cuda.set_device(local)
     threads = os.cpu_count() or 1
     rp, col, w, desc, st = make_graph(args.workload, threads)
+    if args.unweighted:
+        w, desc = None, desc + " (weights dropped: unweighted)"
     V, E = st["V"], st["E"]
     weighted = w is not None and not args.ec
     g = jx.GraphCSRView.from_numpy(rp, col, device=f"cuda:{local}")
@@ -388,6 +390,7 @@ def main():
     ap.add_argument("--impl", default="jx", choices=["jx", "reference"])
     ap.add_argument("--workload", default="rmat24w", choices=["rmat24w", "rmat20", "er4096"])
     ap.add_argument("--ec", action="store_true", help="edge-centric algorithm")
+    ap.add_argument("--unweighted", action="store_true", help="drop the vertex weights")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

@@ -15,8 +15,8 @@
 //
 // Bins by d_u (the staged list), each row list sorted by degree, largest first:
 //   B0  d_u <= 32      one warp per row, one lane per task, 64-slot hash per warp
-//   B1  d_u <= 512     one warp per row, 1024-slot hash per warp (shared memory)
-//   B2  d_u <= 24576   one 1024-thread CTA per row, hash of up to 48K slots (192 KB)
+//   B1  d_u <= 512     one warp per row, cuckoo hash of <= 1280 slots per warp (shared)
+//   B2  d_u <= 24576   one 1024-thread CTA per row, cuckoo hash of <= 58000 slots (227 KB)
 //   hub d_u >  24576   8-CTA clusters; N(u) as a bitmap over [0, n) in global memory (L2)
 //
 // Streaming: a warp reads the ref list in 256-element chunks, lane k holding positions
@@ -25,10 +25,10 @@
 // Weighted sums follow the reference's accumulation order exactly.  On a CPU SYCL device its
 // 8 i-lanes add their matches one lane after another (jaccard.cpp:343, 370-396): ref
 // positions 0, 8, 16, ..., then 1, 9, 17, ..., i.e. "class" c = position mod 8 major,
-// position minor.  Class 0 is folded while streaming; the matched values of classes 1..7 are
-// appended to per-warp class streams (shared memory for B1, global scratch otherwise) and
-// folded class by class after the list ends.  A task whose class stream would overflow is
-// recomputed with a class-major strided walk (same order, no buffering).
+// position minor.  While streaming, the matched values of each class are appended to
+// per-warp class streams (shared memory for B1, global scratch otherwise); after the list
+// ends one lane folds them class by class.  A class that outgrows its stream resumes with a
+// strided walk over its remaining positions (same order).
 #include "jx_common.cuh"
 
 #include <cooperative_groups.h>
@@ -40,7 +40,11 @@ namespace cg = cooperative_groups;
 namespace jx {
 
 constexpr int32_t kB0Max = 32, kB1Max = 512, kB2Max = 24576;
-constexpr int kB0Slots = 64, kB1Slots = 1024, kB2Slots = 49152;
+constexpr int kB0Slots = 64;
+constexpr int kB1Slots = 1280;   // cuckoo, 2.5 slots per element at d = 512
+constexpr int kB2Slots = 58000;  // cuckoo, <= 227 KB; load factor <= 0.424 at d = kB2Max
+constexpr int kCuckooMaxEvict = 64;
+constexpr int kCuckooSeeds = 4;
 constexpr int kB2Threads = 1024;
 constexpr int kRowThreads = 256;
 constexpr int kHubThreads = 1024;
@@ -48,7 +52,9 @@ constexpr int kCluster = 8;
 constexpr int32_t kEmpty = -1;
 constexpr int kChunk = 256;
 constexpr int kB1Cap = kB1Max / 8;   // class-stream capacity per class, B1 (exact bound)
-constexpr int kCap = 2048;           // class-stream capacity per class, B2 / hubs
+constexpr int kB1Warps = kRowThreads / 32;
+constexpr int kCap = (kB2Max + 7) / 8; // class-stream capacity per class, B2 (exact bound)
+constexpr int kHubCap = 8192;          // class-stream capacity per class, hubs (overflow resumes)
 constexpr int kHubTasksPerUnit = 32768;
 constexpr int kKeys = 128;           // plan sort keys: 4 bins x 32 log2 buckets
 constexpr unsigned kClass0 = 0x01010101u;
@@ -93,6 +99,41 @@ struct HashProbe {
   }
 };
 
+// Two-choice cuckoo hash set of N(u) in shared memory: table halves [0, m) and [m, 2m), a key
+// lives at h1(key) or at m + h2(key).  A lookup is two independent loads and no branch, so all
+// lanes of a warp stay converged (linear probing made lanes wait on each other's collision
+// chains).  Inserts run in parallel with atomicExch and a bounded eviction walk; a failed
+// build (an eviction cycle) is retried with other multipliers.
+struct CuckooProbe {
+  const int32_t *t;
+  uint32_t m, a1, a2;
+  __device__ __forceinline__ uint32_t h1(int32_t k) const { return __umulhi((uint32_t)k * a1, m); }
+  __device__ __forceinline__ uint32_t h2(int32_t k) const { return m + __umulhi((uint32_t)k * a2, m); }
+  __device__ __forceinline__ bool operator()(int32_t key) const {
+    const int32_t k1 = t[h1(key)], k2 = t[h2(key)];
+    return (k1 == key) | (k2 == key);
+  }
+};
+
+// Odd multipliers for attempt `seed` (xor with an even number keeps them odd).
+__device__ __forceinline__ CuckooProbe cuckoo_params(const int32_t *t, uint32_t slots, int seed) {
+  return CuckooProbe{t, slots / 2, 0x9E3779B1u ^ ((uint32_t)seed * 0x6A09E668u),
+                     0x85EBCA77u ^ ((uint32_t)seed * 0xBB67AE86u)};
+}
+
+// Inserts `key`; false when the eviction walk gave up (the table then misses a key).
+__device__ __forceinline__ bool cuckoo_insert(const CuckooProbe &c, int32_t *t, int32_t key) {
+  uint32_t loc = c.h1(key);
+  for (int it = 0; it < kCuckooMaxEvict; ++it) {
+    const int32_t old = atomicExch(t + loc, key);
+    if (old == kEmpty || old == key) return true;
+    key = old;
+    const uint32_t l1 = c.h1(key);
+    loc = (loc == l1) ? c.h2(key) : l1;
+  }
+  return false;
+}
+
 // Bitmap of N(u) over [0, n) in global memory, rebuilt per hub: read through L2 only
 // (ld.global.cg), never from a possibly stale L1 line.
 struct BitmapProbe {
@@ -110,23 +151,41 @@ struct SearchProbe {
 };
 
 // ---------------------------------------------------------------- class streams
-// Per-warp storage for the matched values of classes 1..7 (class c at base + (c-1)*cap).
+// Per-warp storage for the matched values of the 8 classes (class c at base + c * cap), in
+// ascending ref position.  After the stream one lane folds them class by class.
 struct ClassStreams {
   float *base;
   int cap;
-  __device__ __forceinline__ void put(int c, int pos, float v) const {
-    if (pos < cap) __stcg(base + (c - 1) * cap + pos, v);
+  __device__ __forceinline__ void put(int c, int pos, float v) const { __stcg(base + c * cap + pos, v); }
+  // acc = v[0] + acc, then v[1] + acc, ... over the first n values of class c (one lane).
+  __device__ __forceinline__ float fold(int c, int n, float acc) const {
+    const float *p = base + c * cap;
+    int i = 0;
+    for (; i + 8 <= n; i += 8) {
+      const float4 a = __ldcg(reinterpret_cast<const float4 *>(p + i));
+      const float4 b = __ldcg(reinterpret_cast<const float4 *>(p + i + 4));
+      acc = a.x + acc; acc = a.y + acc; acc = a.z + acc; acc = a.w + acc;
+      acc = b.x + acc; acc = b.y + acc; acc = b.z + acc; acc = b.w + acc;
+    }
+    for (; i < n; ++i) acc = __ldcg(p + i) + acc;
+    return acc;
   }
-  __device__ __forceinline__ float get(int c, int pos) const { return __ldcg(base + (c - 1) * cap + pos); }
 };
 
 struct SmemClassStreams {
   float *base;
   int cap;
-  __device__ __forceinline__ void put(int c, int pos, float v) const {
-    if (pos < cap) base[(c - 1) * cap + pos] = v;
+  __device__ __forceinline__ void put(int c, int pos, float v) const { base[c * cap + pos] = v; }
+  __device__ __forceinline__ float fold(int c, int n, float acc) const {
+    const float *p = base + c * cap;
+    int i = 0;
+    for (; i + 4 <= n; i += 4) {
+      const float4 a = *reinterpret_cast<const float4 *>(p + i);
+      acc = a.x + acc; acc = a.y + acc; acc = a.z + acc; acc = a.w + acc;
+    }
+    for (; i < n; ++i) acc = p[i] + acc;
+    return acc;
   }
-  __device__ __forceinline__ float get(int c, int pos) const { return base[(c - 1) * cap + pos]; }
 };
 
 // ---------------------------------------------------------------- one task, one warp
@@ -159,9 +218,31 @@ __device__ __forceinline__ float task_strided(const Probe &probe, const int32_t 
   return acc;
 }
 
+// The remaining positions of class c, from p0 (p0 = c mod 8) to the end of the ref list,
+// folded in order onto acc (uniform across the warp): the tail of an overflowing class.
+template <class Probe>
+__device__ __forceinline__ float class_tail(const Probe &probe, const int32_t *__restrict__ col,
+                                            const float *__restrict__ w, int32_t vs, int32_t dv,
+                                            int32_t p0, float acc) {
+  const int lane = threadIdx.x & 31;
+  for (int32_t q = p0; q < dv; q += 32 * kIsILanes) {
+    const int32_t p = q + kIsILanes * lane;
+    bool found = false;
+    float val = 0.0f;
+    if (p < dv) {
+      const int32_t x = __ldg(col + vs + p);
+      found = probe(x);
+      if (found) val = __ldg(w + x);
+    }
+    acc = warp_ordered_fold(__ballot_sync(kFull, found), val, acc);
+  }
+  return acc;
+}
+
 // Chunked stream of N(v) = col[vs, vs+dv) through `probe`.  Returns the intersection value in
 // the reference's order (count when unweighted) and the position of u in N(v) in `mirror`
-// (-1 absent, -2 more than once).
+// (-1 absent, -2 more than once).  Counts and the position of u are kept per lane and
+// reduced once per task.
 template <bool kWeighted, class Probe, class Streams>
 __device__ __forceinline__ float task_stream(const Probe &probe, const int32_t *__restrict__ col,
                                              const float *__restrict__ w, int32_t u, int32_t vs,
@@ -170,10 +251,9 @@ __device__ __forceinline__ float task_stream(const Probe &probe, const int32_t *
   const unsigned lt = (1u << lane) - 1u;
   const int my_class = lane & 7;
   const unsigned my_cmask = kClass0 << my_class;
-  mirror = -1;
-  int32_t cnt = 0;
-  float acc = 0.0f;
+  int32_t cnt = 0, ucnt = 0, upos = -1;
   int32_t ccount = 0; // matches so far in this lane's class (same value in all lanes of a class)
+  int32_t lastp = -1; // ref position of the last value this lane stored
   for (int32_t base = 0; base < dv; base += kChunk) {
     int32_t x[8];
 #pragma unroll
@@ -183,41 +263,51 @@ __device__ __forceinline__ float task_stream(const Probe &probe, const int32_t *
     }
     bool f[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) f[j] = x[j] != kEmpty && probe(x[j]);
-#pragma unroll
     for (int j = 0; j < 8; ++j) {
-      const unsigned mb = __ballot_sync(kFull, x[j] == u && x[j] != kEmpty);
-      if (mb) mirror = (mirror == -1 && __popc(mb) == 1) ? base + 32 * j + __ffs(mb) - 1 : -2;
+      // padding lanes probe vertex 0 (always a valid key) and discard the answer
+      const int32_t key = x[j] != kEmpty ? x[j] : 0;
+      f[j] = (x[j] != kEmpty) & probe(key);
     }
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if (x[j] == u) {
+        ++ucnt;
+        upos = base + lane + 32 * j;
+      }
     if (!kWeighted) {
 #pragma unroll
-      for (int j = 0; j < 8; ++j) cnt += __popc(__ballot_sync(kFull, f[j]));
+      for (int j = 0; j < 8; ++j) cnt += f[j];
     } else {
       // position base + lane + 32j has class (lane & 7); within a class, ascending positions
-      // are j-major, lane-minor: exactly the order of these ballots.
+      // are j-major, lane-minor: the order of these ballots.
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const unsigned m = __ballot_sync(kFull, f[j]);
-        const float val = f[j] ? __ldg(w + x[j]) : 0.0f;
-        acc = warp_ordered_fold(m & kClass0, val, acc);
-        if (f[j] && my_class != 0) cls.put(my_class, ccount + __popc(m & my_cmask & lt), val);
+        if (f[j]) {
+          const int32_t pos = ccount + __popc(m & my_cmask & lt);
+          if (pos < cls.cap) {
+            cls.put(my_class, pos, __ldg(w + x[j]));
+            lastp = base + lane + 32 * j;
+          }
+        }
         ccount += __popc(m & my_cmask);
       }
     }
   }
-  if (!kWeighted) return (float)cnt;
+  const int32_t utot = __reduce_add_sync(kFull, ucnt);
+  mirror = utot == 0 ? -1 : (utot == 1 ? __reduce_max_sync(kFull, upos) : -2);
+  if (!kWeighted) return (float)__reduce_add_sync(kFull, cnt);
   __syncwarp();
-  bool overflow = false;
-  for (int c = 1; c < 8; ++c) overflow |= __shfl_sync(kFull, ccount, c) > cls.cap;
-  if (overflow) return task_strided<true>(probe, col, w, u, vs, dv, mirror);
-  for (int c = 1; c < 8; ++c) {
+  float acc = 0.0f;
+  for (int c = 0; c < 8; ++c) {
     const int32_t nc = __shfl_sync(kFull, ccount, c);
-    for (int32_t t = 0; t < nc; t += 32) {
-      const int32_t k = nc - t < 32 ? nc - t : 32;
-      const float v = lane < k ? cls.get(c, t + lane) : 0.0f;
-      for (int b = 0; b < k; ++b) acc = __shfl_sync(kFull, v, b) + acc;
+    if (lane == 0) acc = cls.fold(c, nc < cls.cap ? nc : cls.cap, acc);
+    if (nc > cls.cap) { // resume class c after its last stored value
+      const int32_t lp = __reduce_max_sync(kFull, my_class == c ? lastp : -1);
+      acc = class_tail(probe, col, w, vs, dv, lp + kIsILanes, __shfl_sync(kFull, acc, 0));
     }
   }
+  acc = __shfl_sync(kFull, acc, 0);
   __syncwarp();
   return acc;
 }
@@ -371,64 +461,116 @@ __global__ void __launch_bounds__(kRowThreads) b0_kernel(
   }
 }
 
+// ---------------------------------------------------------------- task batches
+// Lanes fetch up to 32 candidate tasks (neighbours k0 .. k_end of row u) at once; the warp
+// then runs the ones with d_v <= d_u one by one.
+template <bool kEC, bool kWeighted, class Probe, class Streams>
+__device__ __forceinline__ void run_batch(const Probe &probe, const Streams &cls,
+                                          const int32_t *__restrict__ row_ptr,
+                                          const int32_t *__restrict__ col, const float *__restrict__ w,
+                                          const float *__restrict__ S, int32_t u, int32_t us, int32_t du,
+                                          float Su, int32_t k0, int32_t k_end, float *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  int32_t v = -1, vs = 0, dv = 0;
+  if (k0 + lane < k_end) {
+    v = __ldg(col + us + k0 + lane);
+    vs = __ldg(row_ptr + v);
+    dv = __ldg(row_ptr + v + 1) - vs;
+  }
+  unsigned todo = __ballot_sync(kFull, v >= 0 && dv <= du);
+  while (todo) {
+    const int b = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const int32_t tv = __shfl_sync(kFull, v, b), tvs = __shfl_sync(kFull, vs, b),
+                  tdv = __shfl_sync(kFull, dv, b);
+    int32_t mirror;
+    const float I = task_stream<kWeighted>(probe, col, w, u, tvs, tdv, mirror, cls);
+    if (lane == 0)
+      write_task<kEC, kWeighted>(I, du, tdv, Su, kWeighted ? __ldg(S + tv) : 0.0f, (int64_t)us + k0 + b,
+                                 mirror >= 0 ? (int64_t)tvs + mirror : -1, out);
+  }
+}
+
+// Cuckoo table size for d keys: 2.5 slots per key (even), at most `cap` slots.
+__device__ __forceinline__ uint32_t cuckoo_slots(int32_t d, uint32_t cap) {
+  uint32_t s = ((5u * (uint32_t)d + 3u) / 2u + 1u) & ~1u;
+  s = s < 4u ? 4u : s;
+  return s > cap ? cap : s;
+}
+
 // ---------------------------------------------------------------- B1: warp per row
+// Dynamic shared memory per warp: kB1Slots table slots, then (weighted) 8 * kB1Cap floats.
 template <bool kEC, bool kWeighted>
 __global__ void __launch_bounds__(kRowThreads) b1_kernel(
     const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, const int32_t *__restrict__ cnt,
     float *__restrict__ out) {
-  __shared__ int32_t tables[kRowThreads / 32][kB1Slots];
-  __shared__ float streams[kWeighted ? kRowThreads / 32 : 1][kWeighted ? 7 * kB1Cap : 1];
+  extern __shared__ int32_t b1_smem[];
+  constexpr int kPerWarp = kB1Slots + (kWeighted ? 8 * kB1Cap : 0);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int32_t *t = tables[wid];
-  const SmemClassStreams cls{streams[kWeighted ? wid : 0], kB1Cap};
+  int32_t *t = b1_smem + wid * kPerWarp;
+  const SmemClassStreams cls{reinterpret_cast<float *>(t + kB1Slots), kB1Cap};
   const int32_t r0 = cnt[kOffKeys + 64], r1 = cnt[kOffKeys + 96];
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t i = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < r1; i += nwarps) {
     const int32_t u = rows[i];
     const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
-    const uint32_t size = 2u * (uint32_t)du;
-    for (uint32_t k = lane; k < size; k += 32) t[k] = kEmpty;
-    __syncwarp();
-    for (int32_t k = lane; k < du; k += 32) hset_insert(t, size, __ldg(col + us + k));
-    __syncwarp();
-    const HashProbe probe{t, size};
     const float Su = kWeighted ? __ldg(S + u) : 0.0f;
-    for (int32_t k0 = 0; k0 < du; k0 += 32) {
-      // lanes fetch 32 candidate tasks at once; the warp then runs them one by one
-      int32_t v = -1, vs = 0, dv = 0;
-      if (k0 + lane < du) {
-        v = __ldg(col + us + k0 + lane);
-        vs = __ldg(row_ptr + v);
-        dv = __ldg(row_ptr + v + 1) - vs;
-      }
-      unsigned todo = __ballot_sync(kFull, v >= 0 && dv <= du);
-      while (todo) {
-        const int b = __ffs(todo) - 1;
-        todo &= todo - 1;
-        const int32_t tv = __shfl_sync(kFull, v, b), tvs = __shfl_sync(kFull, vs, b),
-                      tdv = __shfl_sync(kFull, dv, b);
-        int32_t mirror;
-        const float I = task_stream<kWeighted>(probe, col, w, u, tvs, tdv, mirror, cls);
-        if (lane == 0)
-          write_task<kEC, kWeighted>(I, du, tdv, Su, kWeighted ? __ldg(S + tv) : 0.0f, (int64_t)us + k0 + b,
-                                     mirror >= 0 ? (int64_t)tvs + mirror : -1, out);
-      }
+    const uint32_t slots = cuckoo_slots(du, kB1Slots);
+    int seed = 0;
+    for (; seed < kCuckooSeeds; ++seed) {
+      for (uint32_t k = lane; k < slots; k += 32) t[k] = kEmpty;
+      __syncwarp();
+      const CuckooProbe cp = cuckoo_params(t, slots, seed);
+      bool fail = false;
+      for (int32_t k = lane; k < du; k += 32) fail |= !cuckoo_insert(cp, t, __ldg(col + us + k));
+      fail = __any_sync(kFull, fail);
+      __syncwarp();
+      if (!fail) break;
+    }
+    if (seed < kCuckooSeeds) {
+      const CuckooProbe probe = cuckoo_params(t, slots, seed);
+      for (int32_t k0 = 0; k0 < du; k0 += 32)
+        run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, du, out);
+    } else { // eviction cycles with every multiplier: linear probing (load <= 0.4)
+      for (uint32_t k = lane; k < slots; k += 32) t[k] = kEmpty;
+      __syncwarp();
+      for (int32_t k = lane; k < du; k += 32) hset_insert(t, slots, __ldg(col + us + k));
+      __syncwarp();
+      const HashProbe probe{t, slots};
+      for (int32_t k0 = 0; k0 < du; k0 += 32)
+        run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, du, out);
     }
     __syncwarp();
   }
 }
 
 // ---------------------------------------------------------------- B2: CTA per row
+template <bool kEC, bool kWeighted, class Probe>
+__device__ __forceinline__ void b2_tasks(const Probe &probe, const ClassStreams &cls, int32_t *s_task,
+                                         const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
+                                         const float *__restrict__ w, const float *__restrict__ S, int32_t u,
+                                         int32_t us, int32_t du, float *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const float Su = kWeighted ? __ldg(S + u) : 0.0f;
+  for (;;) {
+    int32_t k0 = 0;
+    if (lane == 0) k0 = atomicAdd(s_task, 32);
+    k0 = __shfl_sync(kFull, k0, 0);
+    if (k0 >= du) break;
+    run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, du, out);
+  }
+}
+
 template <bool kEC, bool kWeighted>
 __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
     const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
     float *__restrict__ out, float *__restrict__ scratch) {
   extern __shared__ int32_t table[];
-  __shared__ int32_t s_row, s_task;
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kB2Threads / 32) + wid) * 7 * kCap, kCap};
+  __shared__ int32_t s_row, s_task, s_fail;
+  const int wid = threadIdx.x >> 5;
+  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kB2Threads / 32) + wid) * 8 * kCap, kCap};
   const int32_t r0 = cnt[kOffKeys + 32], r1 = cnt[kOffKeys + 64];
   for (;;) {
     if (threadIdx.x == 0) {
@@ -440,37 +582,29 @@ __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
     if (i >= r1) break;
     const int32_t u = rows[i];
     const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
-    uint32_t size = 4u * (uint32_t)du;
-    size = size > (uint32_t)kB2Slots ? (uint32_t)kB2Slots : size;
-    for (uint32_t k = threadIdx.x; k < size; k += blockDim.x) table[k] = kEmpty;
-    __syncthreads();
-    for (int32_t k = threadIdx.x; k < du; k += blockDim.x) hset_insert(table, size, __ldg(col + us + k));
-    __syncthreads();
-    const HashProbe probe{table, size};
-    const float Su = kWeighted ? __ldg(S + u) : 0.0f;
-    for (;;) {
-      int32_t k0 = 0;
-      if (lane == 0) k0 = atomicAdd(&s_task, 32);
-      k0 = __shfl_sync(kFull, k0, 0);
-      if (k0 >= du) break;
-      int32_t v = -1, vs = 0, dv = 0;
-      if (k0 + lane < du) {
-        v = __ldg(col + us + k0 + lane);
-        vs = __ldg(row_ptr + v);
-        dv = __ldg(row_ptr + v + 1) - vs;
-      }
-      unsigned todo = __ballot_sync(kFull, v >= 0 && dv <= du);
-      while (todo) {
-        const int b = __ffs(todo) - 1;
-        todo &= todo - 1;
-        const int32_t tv = __shfl_sync(kFull, v, b), tvs = __shfl_sync(kFull, vs, b),
-                      tdv = __shfl_sync(kFull, dv, b);
-        int32_t mirror;
-        const float I = task_stream<kWeighted>(probe, col, w, u, tvs, tdv, mirror, cls);
-        if (lane == 0)
-          write_task<kEC, kWeighted>(I, du, tdv, Su, kWeighted ? __ldg(S + tv) : 0.0f, (int64_t)us + k0 + b,
-                                     mirror >= 0 ? (int64_t)tvs + mirror : -1, out);
-      }
+    const uint32_t slots = cuckoo_slots(du, kB2Slots);
+    int seed = 0;
+    for (; seed < kCuckooSeeds; ++seed) {
+      for (uint32_t k = threadIdx.x; k < slots; k += blockDim.x) table[k] = kEmpty;
+      if (threadIdx.x == 0) s_fail = 0;
+      __syncthreads();
+      const CuckooProbe cp = cuckoo_params(table, slots, seed);
+      bool fail = false;
+      for (int32_t k = threadIdx.x; k < du; k += blockDim.x) fail |= !cuckoo_insert(cp, table, __ldg(col + us + k));
+      if (fail) s_fail = 1;
+      __syncthreads();
+      const bool failed = s_fail != 0;
+      __syncthreads();
+      if (!failed) break;
+    }
+    if (seed < kCuckooSeeds) {
+      b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), cls, &s_task, row_ptr, col, w, S, u, us, du, out);
+    } else { // eviction cycles with every multiplier: linear probing (load <= 0.43)
+      for (uint32_t k = threadIdx.x; k < slots; k += blockDim.x) table[k] = kEmpty;
+      __syncthreads();
+      for (int32_t k = threadIdx.x; k < du; k += blockDim.x) hset_insert(table, slots, __ldg(col + us + k));
+      __syncthreads();
+      b2_tasks<kEC, kWeighted>(HashProbe{table, slots}, cls, &s_task, row_ptr, col, w, S, u, us, du, out);
     }
     __syncthreads();
   }
@@ -493,7 +627,7 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
   const int64_t cid = blockIdx.x / kCluster;
   uint32_t *bm = bitmaps + cid * words;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kHubThreads / 32) + wid) * 7 * kCap, kCap};
+  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kHubThreads / 32) + wid) * 8 * kHubCap, kHubCap};
   int32_t *unit_p = cluster.map_shared_rank(&s_unit, 0);
   int32_t *task_p = cluster.map_shared_rank(&s_task, 0);
   const int32_t h0 = cnt[kOffKeys + 0];
@@ -529,24 +663,7 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
       if (lane == 0) k0 = k_begin + atomicAdd(task_p, 32);
       k0 = __shfl_sync(kFull, k0, 0);
       if (k0 >= k_end) break;
-      int32_t v = -1, vs = 0, dv = 0;
-      if (k0 + lane < k_end) {
-        v = __ldg(col + us + k0 + lane);
-        vs = __ldg(row_ptr + v);
-        dv = __ldg(row_ptr + v + 1) - vs;
-      }
-      unsigned todo = __ballot_sync(kFull, v >= 0 && dv <= du);
-      while (todo) {
-        const int b = __ffs(todo) - 1;
-        todo &= todo - 1;
-        const int32_t tv = __shfl_sync(kFull, v, b), tvs = __shfl_sync(kFull, vs, b),
-                      tdv = __shfl_sync(kFull, dv, b);
-        int32_t mirror;
-        const float I = task_stream<kWeighted>(probe, col, w, u, tvs, tdv, mirror, cls);
-        if (lane == 0)
-          write_task<kEC, kWeighted>(I, du, tdv, Su, kWeighted ? __ldg(S + tv) : 0.0f, (int64_t)us + k0 + b,
-                                     mirror >= 0 ? (int64_t)tvs + mirror : -1, out);
-      }
+      run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, k_end, out);
     }
     cluster.sync();
     for (int32_t k = rank * blockDim.x + threadIdx.x; k < du; k += kCluster * blockDim.x)
@@ -637,9 +754,11 @@ static Layout layout(int32_t n, int32_t e, bool weighted_vc) {
   const size_t max_hubs = std::min<size_t>((size_t)n, (size_t)e / (kB2Max + 1));
   L.unit_off = off; off += align256(sizeof(int32_t) * (max_hubs + 2));
   L.S = off;        off += weighted_vc ? align256(sizeof(float) * (size_t)n) : 0;
-  // class streams: one region per warp of the B2 grid (sms CTAs) or the hub grid
-  const size_t warps = (size_t)(sms > L.clusters * kCluster ? sms : L.clusters * kCluster) * 32;
-  L.scratch = off;  off += weighted_vc ? align256(sizeof(float) * warps * 7 * kCap) : 0;
+  // class streams: one region per warp of the B2 grid (sms CTAs) or of the hub grid; the two
+  // kernels run one after the other and share the region
+  const size_t b2_floats = (size_t)sms * (kB2Threads / 32) * 8 * kCap;
+  const size_t hub_floats = (size_t)L.clusters * kCluster * (kHubThreads / 32) * 8 * kHubCap;
+  L.scratch = off;  off += weighted_vc ? align256(sizeof(float) * std::max(b2_floats, hub_floats)) : 0;
   L.bitmaps = off;  off += align256(sizeof(uint32_t) * (size_t)L.words * L.clusters);
   L.total = off;
   return L;
@@ -705,7 +824,10 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
   b2_kernel<kEC, kWeighted><<<sms, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out, scratch);
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("cta_rows", s);
-  b1_kernel<kEC, kWeighted><<<sms * 4, kRowThreads, 0, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
+  const size_t smem_b1 = sizeof(int32_t) * (kRowThreads / 32) * (kB1Slots + (kWeighted ? 8 * kB1Cap : 0));
+  ce = cudaFuncSetAttribute(b1_kernel<kEC, kWeighted>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b1);
+  if (ce != cudaSuccess) return set_cuda_error(ce);
+  b1_kernel<kEC, kWeighted><<<sms * 3, kRowThreads, smem_b1, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("warp_rows", s);
   b0_kernel<kEC, kWeighted><<<sms * 8, kRowThreads, 0, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
