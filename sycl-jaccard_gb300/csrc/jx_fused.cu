@@ -152,41 +152,48 @@ struct SearchProbe {
 
 // ---------------------------------------------------------------- class streams
 // Per-warp storage for the matched values of the 8 classes (class c at base + c * cap), in
-// ascending ref position.  After the stream one lane folds them class by class.
-struct ClassStreams {
+// ascending ref position.  After the stream the warp folds them class by class: all lanes
+// load 128 values at once (one float4 each, the next 128 already in flight), then the values
+// are added one by one in order through shuffles with constant lane indices, so only the
+// add chain itself is serial.  cap is a multiple of 4, so no float4 read leaves the class.
+template <bool kGlobal> struct Streams {
   float *base;
   int cap;
-  __device__ __forceinline__ void put(int c, int pos, float v) const { __stcg(base + c * cap + pos, v); }
-  // acc = v[0] + acc, then v[1] + acc, ... over the first n values of class c (one lane).
+  __device__ __forceinline__ void put(int c, int pos, float v) const {
+    if (kGlobal) __stcg(base + c * cap + pos, v); else base[c * cap + pos] = v;
+  }
+  __device__ __forceinline__ float4 load4(const float *p) const {
+    if (kGlobal) return __ldcg(reinterpret_cast<const float4 *>(p));
+    return *reinterpret_cast<const float4 *>(p);
+  }
+  // acc = v[0] + acc, v[1] + acc, ... over the first n values of class c; acc uniform.
   __device__ __forceinline__ float fold(int c, int n, float acc) const {
+    const int lane = threadIdx.x & 31;
     const float *p = base + c * cap;
-    int i = 0;
-    for (; i + 8 <= n; i += 8) {
-      const float4 a = __ldcg(reinterpret_cast<const float4 *>(p + i));
-      const float4 b = __ldcg(reinterpret_cast<const float4 *>(p + i + 4));
-      acc = a.x + acc; acc = a.y + acc; acc = a.z + acc; acc = a.w + acc;
-      acc = b.x + acc; acc = b.y + acc; acc = b.z + acc; acc = b.w + acc;
+    float4 cur = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (4 * lane < n) cur = load4(p + 4 * lane);
+    for (int t = 0; t < n; t += 128) {
+      float4 nxt = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (t + 128 + 4 * lane < n) nxt = load4(p + t + 128 + 4 * lane);
+      const int k = n - t < 128 ? n - t : 128;
+#pragma unroll
+      for (int L = 0; L < 32; ++L) {
+        if (4 * L < k) {
+          const float a = __shfl_sync(kFull, cur.x, L), b = __shfl_sync(kFull, cur.y, L);
+          const float q = __shfl_sync(kFull, cur.z, L), d = __shfl_sync(kFull, cur.w, L);
+          acc = a + acc;
+          if (4 * L + 1 < k) acc = b + acc;
+          if (4 * L + 2 < k) acc = q + acc;
+          if (4 * L + 3 < k) acc = d + acc;
+        }
+      }
+      cur = nxt;
     }
-    for (; i < n; ++i) acc = __ldcg(p + i) + acc;
     return acc;
   }
 };
-
-struct SmemClassStreams {
-  float *base;
-  int cap;
-  __device__ __forceinline__ void put(int c, int pos, float v) const { base[c * cap + pos] = v; }
-  __device__ __forceinline__ float fold(int c, int n, float acc) const {
-    const float *p = base + c * cap;
-    int i = 0;
-    for (; i + 4 <= n; i += 4) {
-      const float4 a = *reinterpret_cast<const float4 *>(p + i);
-      acc = a.x + acc; acc = a.y + acc; acc = a.z + acc; acc = a.w + acc;
-    }
-    for (; i < n; ++i) acc = p[i] + acc;
-    return acc;
-  }
-};
+using ClassStreams = Streams<true>;
+using SmemClassStreams = Streams<false>;
 
 // ---------------------------------------------------------------- one task, one warp
 // Class-major strided walk (the reference's order with no buffering); used for overflowing
@@ -239,75 +246,90 @@ __device__ __forceinline__ float class_tail(const Probe &probe, const int32_t *_
   return acc;
 }
 
+// One 256-element chunk at `base`: lane k takes positions base + k + 32j.  kTail: the chunk
+// may run past the end of the list (bounds checks; padding lanes probe vertex 0, always a
+// valid key, and drop the answer).
+template <bool kWeighted, bool kTail, class Probe, class Streams>
+__device__ __forceinline__ void task_chunk(const Probe &probe, const int32_t *__restrict__ col,
+                                           const float *__restrict__ w, int32_t u, int32_t vs,
+                                           int32_t dv, int32_t base, const Streams &cls, int32_t &cnt,
+                                           int32_t &upos, int32_t &ccount, int32_t &lastp) {
+  const int lane = threadIdx.x & 31;
+  int32_t x[8];
+  bool f[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int32_t p = base + lane + 32 * j;
+    x[j] = (!kTail || p < dv) ? __ldg(col + vs + p) : kEmpty;
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    if (kTail) {
+      const int32_t key = x[j] != kEmpty ? x[j] : 0;
+      f[j] = (x[j] != kEmpty) & probe(key);
+    } else {
+      f[j] = probe(x[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 8; ++j)
+    if (x[j] == u) upos = base + lane + 32 * j;
+  if (!kWeighted) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) cnt += f[j];
+  } else {
+    // position base + lane + 32j has class (lane & 7); within a class, ascending positions
+    // are j-major, lane-minor: the order of these ballots.
+    const unsigned lt = (1u << lane) - 1u;
+    const int my_class = lane & 7;
+    const unsigned my_cmask = kClass0 << my_class;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const unsigned m = __ballot_sync(kFull, f[j]);
+      if (f[j]) {
+        const int32_t pos = ccount + __popc(m & my_cmask & lt);
+        if (pos < cls.cap) {
+          cls.put(my_class, pos, __ldg(w + x[j]));
+          lastp = base + lane + 32 * j;
+        }
+      }
+      ccount += __popc(m & my_cmask);
+    }
+  }
+}
+
 // Chunked stream of N(v) = col[vs, vs+dv) through `probe`.  Returns the intersection value in
-// the reference's order (count when unweighted) and the position of u in N(v) in `mirror`
-// (-1 absent, -2 more than once).  Counts and the position of u are kept per lane and
-// reduced once per task.
+// the reference's order (count when unweighted) and a position of u in N(v) in `mirror`
+// (-1 absent).  Counts and the position of u are kept per lane and reduced once per task.
 template <bool kWeighted, class Probe, class Streams>
 __device__ __forceinline__ float task_stream(const Probe &probe, const int32_t *__restrict__ col,
                                              const float *__restrict__ w, int32_t u, int32_t vs,
                                              int32_t dv, int32_t &mirror, const Streams &cls) {
   const int lane = threadIdx.x & 31;
-  const unsigned lt = (1u << lane) - 1u;
   const int my_class = lane & 7;
-  const unsigned my_cmask = kClass0 << my_class;
-  int32_t cnt = 0, ucnt = 0, upos = -1;
+  int32_t cnt = 0, upos = -1;
   int32_t ccount = 0; // matches so far in this lane's class (same value in all lanes of a class)
   int32_t lastp = -1; // ref position of the last value this lane stored
-  for (int32_t base = 0; base < dv; base += kChunk) {
-    int32_t x[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int32_t p = base + lane + 32 * j;
-      x[j] = p < dv ? __ldg(col + vs + p) : kEmpty;
-    }
-    bool f[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      // padding lanes probe vertex 0 (always a valid key) and discard the answer
-      const int32_t key = x[j] != kEmpty ? x[j] : 0;
-      f[j] = (x[j] != kEmpty) & probe(key);
-    }
-#pragma unroll
-    for (int j = 0; j < 8; ++j)
-      if (x[j] == u) {
-        ++ucnt;
-        upos = base + lane + 32 * j;
-      }
-    if (!kWeighted) {
-#pragma unroll
-      for (int j = 0; j < 8; ++j) cnt += f[j];
-    } else {
-      // position base + lane + 32j has class (lane & 7); within a class, ascending positions
-      // are j-major, lane-minor: the order of these ballots.
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const unsigned m = __ballot_sync(kFull, f[j]);
-        if (f[j]) {
-          const int32_t pos = ccount + __popc(m & my_cmask & lt);
-          if (pos < cls.cap) {
-            cls.put(my_class, pos, __ldg(w + x[j]));
-            lastp = base + lane + 32 * j;
-          }
-        }
-        ccount += __popc(m & my_cmask);
-      }
-    }
-  }
-  const int32_t utot = __reduce_add_sync(kFull, ucnt);
-  mirror = utot == 0 ? -1 : (utot == 1 ? __reduce_max_sync(kFull, upos) : -2);
+  int32_t base = 0;
+  for (; base + kChunk <= dv; base += kChunk)
+    task_chunk<kWeighted, false>(probe, col, w, u, vs, dv, base, cls, cnt, upos, ccount, lastp);
+  if (base < dv)
+    task_chunk<kWeighted, true>(probe, col, w, u, vs, dv, base, cls, cnt, upos, ccount, lastp);
+  // Position of u in N(v).  If u occurs more than once (a repeated neighbour), the task's
+  // value is right for every occurrence; the one written here is the last, the others keep
+  // the sentinel and the fix-up pass computes them.
+  mirror = __reduce_max_sync(kFull, upos);
   if (!kWeighted) return (float)__reduce_add_sync(kFull, cnt);
   __syncwarp();
   float acc = 0.0f;
   for (int c = 0; c < 8; ++c) {
     const int32_t nc = __shfl_sync(kFull, ccount, c);
-    if (lane == 0) acc = cls.fold(c, nc < cls.cap ? nc : cls.cap, acc);
+    acc = cls.fold(c, nc < cls.cap ? nc : cls.cap, acc);
     if (nc > cls.cap) { // resume class c after its last stored value
       const int32_t lp = __reduce_max_sync(kFull, my_class == c ? lastp : -1);
-      acc = class_tail(probe, col, w, vs, dv, lp + kIsILanes, __shfl_sync(kFull, acc, 0));
+      acc = class_tail(probe, col, w, vs, dv, lp + kIsILanes, acc);
     }
   }
-  acc = __shfl_sync(kFull, acc, 0);
   __syncwarp();
   return acc;
 }
