@@ -257,6 +257,10 @@ def run_gpu(args, world, rank, local):
     rp, col, w, desc, st = make_graph(args.workload, threads)
     if args.unweighted:
         w, desc = None, desc + " (weights dropped: unweighted)"
+    elif args.weighted and w is None:
+        jx = importlib.import_module("sycl-jaccard_gb300")
+        w = jx.graphgen.uniform_weights(st["V"], seed=4, threads=threads)
+        desc += " + vertex weights U(0,1] seed 4"
     V, E = st["V"], st["E"]
     weighted = w is not None and not args.ec
     g = jx.GraphCSRView.from_numpy(rp, col, device=f"cuda:{local}")
@@ -391,6 +395,8 @@ def main():
     ap.add_argument("--workload", default="rmat24w", choices=["rmat24w", "rmat20", "er4096"])
     ap.add_argument("--ec", action="store_true", help="edge-centric algorithm")
     ap.add_argument("--unweighted", action="store_true", help="drop the vertex weights")
+    ap.add_argument("--weighted", action="store_true",
+                    help="add U(0,1] vertex weights (seed 4) to a workload that has none")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

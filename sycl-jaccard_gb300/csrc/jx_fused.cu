@@ -151,36 +151,42 @@ struct SearchProbe {
 };
 
 // ---------------------------------------------------------------- class streams
-// Per-warp storage for the matched values of the 8 classes (class c at base + c * cap), in
-// ascending ref position.  After the stream the warp folds them class by class: all lanes
-// load 128 values at once (one float4 each, the next 128 already in flight), then the values
-// are added one by one in order through shuffles with constant lane indices, so only the
-// add chain itself is serial.  cap is a multiple of 4, so no float4 read leaves the class.
+// Per-warp storage for the matched vertex ids of the 8 classes (class c at base + c * cap),
+// in ascending ref position.  The weights are gathered only when the warp folds the classes:
+// all lanes load 128 ids at once (one int4 each, the next 128 already in flight) and gather
+// their 4 weights, then the values are added one by one in order through shuffles with
+// constant lane indices, so only the add chain itself is serial.  cap is a multiple of 4, so
+// no int4 read leaves its class.
 template <bool kGlobal> struct Streams {
-  float *base;
+  int32_t *base;
   int cap;
-  __device__ __forceinline__ void put(int c, int pos, float v) const {
-    if (kGlobal) __stcg(base + c * cap + pos, v); else base[c * cap + pos] = v;
+  __device__ __forceinline__ void put(int c, int pos, int32_t x) const {
+    if (kGlobal) __stcg(base + c * cap + pos, x); else base[c * cap + pos] = x;
   }
-  __device__ __forceinline__ float4 load4(const float *p) const {
-    if (kGlobal) return __ldcg(reinterpret_cast<const float4 *>(p));
-    return *reinterpret_cast<const float4 *>(p);
+  __device__ __forceinline__ int4 load4(const int32_t *p) const {
+    if (kGlobal) return __ldcg(reinterpret_cast<const int4 *>(p));
+    return *reinterpret_cast<const int4 *>(p);
   }
-  // acc = v[0] + acc, v[1] + acc, ... over the first n values of class c; acc uniform.
-  __device__ __forceinline__ float fold(int c, int n, float acc) const {
+  // acc = w[x0] + acc, w[x1] + acc, ... over the first n ids of class c; acc uniform.
+  __device__ __forceinline__ float fold(int c, int n, const float *__restrict__ w, float acc) const {
     const int lane = threadIdx.x & 31;
-    const float *p = base + c * cap;
-    float4 cur = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int32_t *p = base + c * cap;
+    int4 cur = make_int4(0, 0, 0, 0);
     if (4 * lane < n) cur = load4(p + 4 * lane);
     for (int t = 0; t < n; t += 128) {
-      float4 nxt = make_float4(0.f, 0.f, 0.f, 0.f);
+      int4 nxt = make_int4(0, 0, 0, 0);
       if (t + 128 + 4 * lane < n) nxt = load4(p + t + 128 + 4 * lane);
       const int k = n - t < 128 ? n - t : 128;
+      const int i0 = 4 * lane;
+      const float va = i0 < k ? __ldg(w + cur.x) : 0.0f;
+      const float vb = i0 + 1 < k ? __ldg(w + cur.y) : 0.0f;
+      const float vc = i0 + 2 < k ? __ldg(w + cur.z) : 0.0f;
+      const float vd = i0 + 3 < k ? __ldg(w + cur.w) : 0.0f;
 #pragma unroll
       for (int L = 0; L < 32; ++L) {
         if (4 * L < k) {
-          const float a = __shfl_sync(kFull, cur.x, L), b = __shfl_sync(kFull, cur.y, L);
-          const float q = __shfl_sync(kFull, cur.z, L), d = __shfl_sync(kFull, cur.w, L);
+          const float a = __shfl_sync(kFull, va, L), b = __shfl_sync(kFull, vb, L);
+          const float q = __shfl_sync(kFull, vc, L), d = __shfl_sync(kFull, vd, L);
           acc = a + acc;
           if (4 * L + 1 < k) acc = b + acc;
           if (4 * L + 2 < k) acc = q + acc;
@@ -289,7 +295,7 @@ __device__ __forceinline__ void task_chunk(const Probe &probe, const int32_t *__
       if (f[j]) {
         const int32_t pos = ccount + __popc(m & my_cmask & lt);
         if (pos < cls.cap) {
-          cls.put(my_class, pos, __ldg(w + x[j]));
+          cls.put(my_class, pos, x[j]);
           lastp = base + lane + 32 * j;
         }
       }
@@ -324,7 +330,7 @@ __device__ __forceinline__ float task_stream(const Probe &probe, const int32_t *
   float acc = 0.0f;
   for (int c = 0; c < 8; ++c) {
     const int32_t nc = __shfl_sync(kFull, ccount, c);
-    acc = cls.fold(c, nc < cls.cap ? nc : cls.cap, acc);
+    acc = cls.fold(c, nc < cls.cap ? nc : cls.cap, w, acc);
     if (nc > cls.cap) { // resume class c after its last stored value
       const int32_t lp = __reduce_max_sync(kFull, my_class == c ? lastp : -1);
       acc = class_tail(probe, col, w, vs, dv, lp + kIsILanes, acc);
@@ -531,7 +537,7 @@ __global__ void __launch_bounds__(kRowThreads) b1_kernel(
   constexpr int kPerWarp = kB1Slots + (kWeighted ? 8 * kB1Cap : 0);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   int32_t *t = b1_smem + wid * kPerWarp;
-  const SmemClassStreams cls{reinterpret_cast<float *>(t + kB1Slots), kB1Cap};
+  const SmemClassStreams cls{t + kB1Slots, kB1Cap};
   const int32_t r0 = cnt[kOffKeys + 64], r1 = cnt[kOffKeys + 96];
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t i = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < r1; i += nwarps) {
@@ -592,7 +598,7 @@ __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
   extern __shared__ int32_t table[];
   __shared__ int32_t s_row, s_task, s_fail;
   const int wid = threadIdx.x >> 5;
-  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kB2Threads / 32) + wid) * 8 * kCap, kCap};
+  const ClassStreams cls{reinterpret_cast<int32_t *>(scratch) + ((int64_t)blockIdx.x * (kB2Threads / 32) + wid) * 8 * kCap, kCap};
   const int32_t r0 = cnt[kOffKeys + 32], r1 = cnt[kOffKeys + 64];
   for (;;) {
     if (threadIdx.x == 0) {
@@ -649,7 +655,7 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
   const int64_t cid = blockIdx.x / kCluster;
   uint32_t *bm = bitmaps + cid * words;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kHubThreads / 32) + wid) * 8 * kHubCap, kHubCap};
+  const ClassStreams cls{reinterpret_cast<int32_t *>(scratch) + ((int64_t)blockIdx.x * (kHubThreads / 32) + wid) * 8 * kHubCap, kHubCap};
   int32_t *unit_p = cluster.map_shared_rank(&s_unit, 0);
   int32_t *task_p = cluster.map_shared_rank(&s_task, 0);
   const int32_t h0 = cnt[kOffKeys + 0];
