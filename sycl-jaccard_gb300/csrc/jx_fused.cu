@@ -163,6 +163,9 @@ template <bool kGlobal> struct Streams {
   __device__ __forceinline__ void put(int c, int pos, int32_t x) const {
     if (kGlobal) __stcg(base + c * cap + pos, x); else base[c * cap + pos] = x;
   }
+  __device__ __forceinline__ int32_t get(int c, int pos) const {
+    return kGlobal ? __ldcg(base + c * cap + pos) : base[c * cap + pos];
+  }
   __device__ __forceinline__ int4 load4(const int32_t *p) const {
     if (kGlobal) return __ldcg(reinterpret_cast<const int4 *>(p));
     return *reinterpret_cast<const int4 *>(p);
@@ -198,6 +201,50 @@ template <bool kGlobal> struct Streams {
     return acc;
   }
 };
+// All classes at once when none overflowed: lane i takes the i-th matched id in class-major
+// order (class c starts at the prefix sum of the counts of classes < c), gathers its weight,
+// and the warp folds 32 values per round in order.  counts: lane c (c < 8) holds class c's
+// count, other lanes 0.  acc uniform.
+template <class S>
+__device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, const float *__restrict__ w,
+                                          float acc) {
+  const int lane = threadIdx.x & 31;
+  int32_t incl = my_count;
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) {
+    const int32_t y = __shfl_up_sync(kFull, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int32_t total = __shfl_sync(kFull, incl, 7);
+  int32_t start[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) start[c] = __shfl_sync(kFull, incl - my_count, c);
+  for (int32_t t = 0; t < total; t += 32) {
+    const int32_t i = t + lane;
+    float v = 0.0f;
+    if (i < total) {
+      int c = 0;
+      int32_t sc = 0;
+#pragma unroll
+      for (int q = 1; q < 8; ++q)
+        if (i >= start[q]) {
+          c = q;
+          sc = start[q];
+        }
+      v = __ldg(w + cls.get(c, i - sc));
+    }
+    const int32_t k = total - t < 32 ? total - t : 32;
+    int b = 0;
+    for (; b + 4 <= k; b += 4) {
+      const float v0 = __shfl_sync(kFull, v, b), v1 = __shfl_sync(kFull, v, b + 1);
+      const float v2 = __shfl_sync(kFull, v, b + 2), v3 = __shfl_sync(kFull, v, b + 3);
+      acc = v0 + acc; acc = v1 + acc; acc = v2 + acc; acc = v3 + acc;
+    }
+    for (; b < k; ++b) acc = __shfl_sync(kFull, v, b) + acc;
+  }
+  return acc;
+}
+
 using ClassStreams = Streams<true>;
 using SmemClassStreams = Streams<false>;
 
@@ -328,6 +375,11 @@ __device__ __forceinline__ float task_stream(const Probe &probe, const int32_t *
   if (!kWeighted) return (float)__reduce_add_sync(kFull, cnt);
   __syncwarp();
   float acc = 0.0f;
+  if (!__any_sync(kFull, ccount > cls.cap)) {
+    acc = fold_all(cls, lane < 8 ? ccount : 0, w, acc);
+    __syncwarp();
+    return acc;
+  }
   for (int c = 0; c < 8; ++c) {
     const int32_t nc = __shfl_sync(kFull, ccount, c);
     acc = cls.fold(c, nc < cls.cap ? nc : cls.cap, w, acc);
