@@ -53,7 +53,7 @@ constexpr int32_t kEmpty = -1;
 constexpr int kChunk = 256;
 constexpr int kB1Cap = kB1Max / 8;   // class-stream capacity per class, B1 (exact bound)
 constexpr int kB1Warps = kRowThreads / 32;
-constexpr int kCap = (kB2Max + 7) / 8; // class-stream capacity per class, B2 (exact bound)
+constexpr int kCap = (kB2Max + 7) / 8; // class-stream capacity per class, B2 (no overflow)
 constexpr int kHubCap = 8192;          // class-stream capacity per class, hubs (overflow resumes)
 constexpr int kHubTasksPerUnit = 32768;
 constexpr int kKeys = 128;           // plan sort keys: 4 bins x 32 log2 buckets
@@ -646,11 +646,11 @@ template <bool kEC, bool kWeighted>
 __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
     const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
-    float *__restrict__ out, float *__restrict__ scratch) {
+    float *__restrict__ out, int32_t *__restrict__ scratch, int cap) {
   extern __shared__ int32_t table[];
   __shared__ int32_t s_row, s_task, s_fail;
   const int wid = threadIdx.x >> 5;
-  const ClassStreams cls{reinterpret_cast<int32_t *>(scratch) + ((int64_t)blockIdx.x * (kB2Threads / 32) + wid) * 8 * kCap, kCap};
+  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kB2Threads / 32) + wid) * 8 * cap, cap};
   const int32_t r0 = cnt[kOffKeys + 32], r1 = cnt[kOffKeys + 64];
   for (;;) {
     if (threadIdx.x == 0) {
@@ -700,14 +700,14 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
     const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
     const int32_t *__restrict__ unit_off, uint32_t *__restrict__ bitmaps, int64_t words,
-    float *__restrict__ out, float *__restrict__ scratch) {
+    float *__restrict__ out, int32_t *__restrict__ scratch, int cap) {
   cg::cluster_group cluster = cg::this_cluster();
   __shared__ int32_t s_unit, s_task;
   const unsigned rank = cluster.block_rank();
   const int64_t cid = blockIdx.x / kCluster;
   uint32_t *bm = bitmaps + cid * words;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const ClassStreams cls{reinterpret_cast<int32_t *>(scratch) + ((int64_t)blockIdx.x * (kHubThreads / 32) + wid) * 8 * kHubCap, kHubCap};
+  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kHubThreads / 32) + wid) * 8 * cap, cap};
   int32_t *unit_p = cluster.map_shared_rank(&s_unit, 0);
   int32_t *task_p = cluster.map_shared_rank(&s_task, 0);
   const int32_t h0 = cnt[kOffKeys + 0];
@@ -816,16 +816,26 @@ __global__ void __launch_bounds__(256) fixup_kernel(int32_t n, int64_t e, const 
 // ---------------------------------------------------------------- host driver
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// Grid sizes and class-stream capacities of one operator call.  The default plan fills the
+// GPU; the fixed-scratch entry point uses a small plan whose workspace fits its array.
+struct Plan {
+  int b2_ctas;      // CTAs of the B2 kernel (one class-stream region per warp)
+  int hub_clusters; // 8-CTA clusters of the hub kernel (one bitmap slot each)
+  int cap_b2, cap_hub;
+};
+
+static Plan default_plan() {
+  const int sms = sm_count();
+  return Plan{sms, sms / kCluster > 0 ? sms / kCluster : 1, kCap, kHubCap};
+}
+
 struct Layout {
   size_t cnt, rows, unit_off, S, scratch, bitmaps, total;
   int64_t words;
-  int clusters;
 };
 
-static Layout layout(int32_t n, int32_t e, bool weighted_vc) {
+static Layout layout(int32_t n, int32_t e, bool weighted_vc, const Plan &P) {
   Layout L;
-  const int sms = sm_count();
-  L.clusters = sms / kCluster > 0 ? sms / kCluster : 1;
   L.words = ((int64_t)n + 31) / 32;
   size_t off = 0;
   L.cnt = off;      off += align256(sizeof(int32_t) * kCounters);
@@ -834,32 +844,33 @@ static Layout layout(int32_t n, int32_t e, bool weighted_vc) {
   const size_t max_hubs = std::min<size_t>((size_t)n, (size_t)e / (kB2Max + 1));
   L.unit_off = off; off += align256(sizeof(int32_t) * (max_hubs + 2));
   L.S = off;        off += weighted_vc ? align256(sizeof(float) * (size_t)n) : 0;
-  // class streams: one region per warp of the B2 grid (sms CTAs) or of the hub grid; the two
-  // kernels run one after the other and share the region
-  const size_t b2_floats = (size_t)sms * (kB2Threads / 32) * 8 * kCap;
-  const size_t hub_floats = (size_t)L.clusters * kCluster * (kHubThreads / 32) * 8 * kHubCap;
-  L.scratch = off;  off += weighted_vc ? align256(sizeof(float) * std::max(b2_floats, hub_floats)) : 0;
-  L.bitmaps = off;  off += align256(sizeof(uint32_t) * (size_t)L.words * L.clusters);
+  // class streams: one region per warp of the B2 grid or of the hub grid; the two kernels
+  // run one after the other and share the region
+  const size_t b2_ids = (size_t)P.b2_ctas * (kB2Threads / 32) * 8 * P.cap_b2;
+  const size_t hub_ids = (size_t)P.hub_clusters * kCluster * (kHubThreads / 32) * 8 * P.cap_hub;
+  L.scratch = off;  off += weighted_vc ? align256(sizeof(int32_t) * std::max(b2_ids, hub_ids)) : 0;
+  L.bitmaps = off;  off += align256(sizeof(uint32_t) * (size_t)L.words * P.hub_clusters);
   L.total = off;
   return L;
 }
 
 template <bool kEC, bool kWeighted>
-static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws, cudaStream_t s) {
+static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws, const Plan &P,
+                           cudaStream_t s) {
   const int32_t n = g.n;
-  const Layout L = layout(n, g.e, kWeighted);
+  const Layout L = layout(n, g.e, kWeighted, P);
   int32_t *cnt = reinterpret_cast<int32_t *>(ws + L.cnt);
   int32_t *rows = reinterpret_cast<int32_t *>(ws + L.rows);
   int32_t *unit_off = reinterpret_cast<int32_t *>(ws + L.unit_off);
   float *S = kWeighted ? reinterpret_cast<float *>(ws + L.S) : nullptr;
-  float *scratch = kWeighted ? reinterpret_cast<float *>(ws + L.scratch) : nullptr;
+  int32_t *scratch = kWeighted ? reinterpret_cast<int32_t *>(ws + L.scratch) : nullptr;
   uint32_t *bitmaps = reinterpret_cast<uint32_t *>(ws + L.bitmaps);
   const int sms = sm_count();
   jx_status st;
   cudaError_t ce;
   prof_mark("start", s);
   if ((ce = cudaMemsetAsync(cnt, 0, sizeof(int32_t) * kCounters, s)) != cudaSuccess) return set_cuda_error(ce);
-  if ((ce = cudaMemsetAsync(bitmaps, 0, sizeof(uint32_t) * (size_t)L.words * L.clusters, s)) != cudaSuccess)
+  if ((ce = cudaMemsetAsync(bitmaps, 0, sizeof(uint32_t) * (size_t)L.words * P.hub_clusters, s)) != cudaSuccess)
     return set_cuda_error(ce);
   plan_kernel<false><<<sms * 4, 256, 0, s>>>(n, g.row_ptr, cnt, rows);
   if ((st = check_launch()) != JX_OK) return st;
@@ -880,7 +891,7 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
 
   {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(L.clusters * kCluster);
+    cfg.gridDim = dim3(P.hub_clusters * kCluster);
     cfg.blockDim = dim3(kHubThreads);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = s;
@@ -893,7 +904,7 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
     cfg.numAttrs = 1;
     ce = cudaLaunchKernelEx(&cfg, hub_kernel<kEC, kWeighted>, (const int32_t *)g.row_ptr,
                             (const int32_t *)g.col_idx, w, (const float *)S, (const int32_t *)rows, cnt,
-                            (const int32_t *)unit_off, bitmaps, (int64_t)L.words, out, scratch);
+                            (const int32_t *)unit_off, bitmaps, (int64_t)L.words, out, scratch, P.cap_hub);
     if (ce != cudaSuccess) return set_cuda_error(ce);
     if ((st = check_launch()) != JX_OK) return st;
     prof_mark("hub_rows", s);
@@ -901,7 +912,8 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
   const size_t smem_b2 = sizeof(int32_t) * (size_t)kB2Slots;
   ce = cudaFuncSetAttribute(b2_kernel<kEC, kWeighted>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b2);
   if (ce != cudaSuccess) return set_cuda_error(ce);
-  b2_kernel<kEC, kWeighted><<<sms, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out, scratch);
+  b2_kernel<kEC, kWeighted><<<P.b2_ctas, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out,
+                                                                   scratch, P.cap_b2);
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("cta_rows", s);
   const size_t smem_b1 = sizeof(int32_t) * (kRowThreads / 32) * (kB1Slots + (kWeighted ? 8 * kB1Cap : 0));
@@ -919,6 +931,24 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
   return JX_OK;
 }
 
+// Argument checks shared by the entry points; JX_OK with *run = false means "nothing to do".
+static jx_status check_args(const jx_csr *g, jx_algo algo, const float *out_j, bool *run) {
+  *run = false;
+  if (!g || g->n < 0 || g->e < 0) return JX_ERR_INVALID;
+  if (algo != JX_ALGO_VERTEX_CENTRIC && algo != JX_ALGO_EDGE_CENTRIC) return JX_ERR_INVALID;
+  if (g->n == 0 || g->e == 0) return JX_OK;
+  if (!g->row_ptr || !g->col_idx || !out_j) return JX_ERR_INVALID;
+  *run = true;
+  return JX_OK;
+}
+
+static jx_status dispatch(const jx_csr &g, const float *vertex_w, float *out_j, jx_algo algo, char *ws,
+                          const Plan &P, cudaStream_t s) {
+  if (algo == JX_ALGO_EDGE_CENTRIC) return run_fused<true, false>(g, nullptr, out_j, ws, P, s);
+  if (vertex_w) return run_fused<false, true>(g, vertex_w, out_j, ws, P, s);
+  return run_fused<false, false>(g, nullptr, out_j, ws, P, s);
+}
+
 } // namespace jx
 
 using namespace jx;
@@ -927,25 +957,21 @@ extern "C" {
 
 size_t jx_jaccard_workspace_size(const jx_csr *g, int weighted, jx_algo algo) {
   if (!g || g->n < 0) return 0;
-  return layout(g->n, g->e, weighted && algo == JX_ALGO_VERTEX_CENTRIC).total;
+  return layout(g->n, g->e, weighted && algo == JX_ALGO_VERTEX_CENTRIC, default_plan()).total;
 }
 
 jx_status jx_jaccard_ws(const jx_csr *g, const float *vertex_w, float *out_j, jx_algo algo,
                         void *workspace, size_t workspace_bytes, jx_stream_t stream) {
-  if (!g || g->n < 0 || g->e < 0) return JX_ERR_INVALID;
-  if (algo != JX_ALGO_VERTEX_CENTRIC && algo != JX_ALGO_EDGE_CENTRIC) return JX_ERR_INVALID;
-  if (g->n == 0 || g->e == 0) return JX_OK;
-  if (!g->row_ptr || !g->col_idx || !out_j) return JX_ERR_INVALID;
-  const bool ec = algo == JX_ALGO_EDGE_CENTRIC;
-  const bool weighted = vertex_w != nullptr && !ec; // EC ignores weights (jaccard.cpp:790)
-  if (!workspace || workspace_bytes < layout(g->n, g->e, weighted).total ||
+  bool run;
+  const jx_status st = check_args(g, algo, out_j, &run);
+  if (!run) return st;
+  const bool weighted = vertex_w != nullptr && algo == JX_ALGO_VERTEX_CENTRIC; // EC ignores weights
+  const Plan P = default_plan();
+  if (!workspace || workspace_bytes < layout(g->n, g->e, weighted, P).total ||
       (reinterpret_cast<uintptr_t>(workspace) & 255u))
     return JX_ERR_INVALID;
-  char *ws = static_cast<char *>(workspace);
-  cudaStream_t s = (cudaStream_t)stream;
-  if (ec) return run_fused<true, false>(*g, nullptr, out_j, ws, s);
-  if (weighted) return run_fused<false, true>(*g, vertex_w, out_j, ws, s);
-  return run_fused<false, false>(*g, nullptr, out_j, ws, s);
+  return dispatch(*g, weighted ? vertex_w : nullptr, out_j, algo, static_cast<char *>(workspace), P,
+                  (cudaStream_t)stream);
 }
 
 jx_status jx_jaccard(const jx_csr *g, const float *vertex_w, float *out_j, jx_algo algo,
