@@ -99,6 +99,27 @@ jx_status jx_jaccard_ws(const jx_csr *g, const float *vertex_w, float *out_j, jx
 jx_status jx_jaccard_host(int32_t n, int32_t e, const int32_t *row_ptr, const int32_t *col_idx,
                           const float *vertex_w, float *out_j, jx_algo algo);
 
+/*
+ * jx_jaccard without any device allocation.  (No counterpart in the reference.)
+ *
+ * For callers that cannot allocate device memory while they run: services that reserve their
+ * whole device-memory budget up front and own no allocator, and pipelines in which an
+ * allocation call, with the device synchronisation it may bring, is not acceptable between
+ * launches.  The operator, its arguments and its results are those of jx_jaccard; the
+ * workspace is a fixed array of JX_NOALLOC_SCRATCH_BYTES inside this library (every GPU that
+ * loads the library holds it until the process exits), sized for graphs of at most
+ * JX_NOALLOC_MAX_VERTICES vertices; larger graphs are rejected with JX_ERR_TOO_LARGE.
+ * The first call on a device looks up the array's device address (a host-side set-up step);
+ * make that first call before any stream capture.  Every call shares the one array: calls
+ * that overlap on the GPU (on different streams, or from different threads) race and must be
+ * serialised by the caller.  Asynchronous on `stream`; the work is smaller-grid than
+ * jx_jaccard and so slower on large graphs.
+ */
+#define JX_NOALLOC_MAX_VERTICES (1 << 20)
+#define JX_NOALLOC_SCRATCH_BYTES (32u << 20)
+jx_status jx_jaccard_noalloc(const jx_csr *g, const float *vertex_w, float *out_j, jx_algo algo,
+                             jx_stream_t stream);
+
 /* ------------------------------------------------------------------ stage-level calls
  * One call per reference kernel (the static invoke functions of jaccard.hpp), for stage
  * parity and for callers that, like main.cpp:255-257, drive the kernels themselves.

@@ -27,7 +27,7 @@ import numpy as np
 from . import build as _build
 from . import graphgen  # noqa: F401  (synthetic graphs)
 
-__all__ = ["GraphCSRView", "JxError", "jaccard", "jaccard_host", "rowsum", "fill", "intersect",
+__all__ = ["GraphCSRView", "JxError", "jaccard", "jaccard_host", "jaccard_noalloc", "rowsum", "fill", "intersect",
            "weight", "ec_scan", "ec_unweighted", "csr_check", "lib", "launch_count",
            "launch_count_reset", "graphgen"]
 
@@ -76,6 +76,7 @@ def lib() -> ctypes.CDLL:
             "jx_jaccard_ws": ([ctypes.POINTER(_Csr), _VP, _VP, ctypes.c_int, _VP, ctypes.c_size_t, _VP], ctypes.c_int),
             "jx_jaccard_workspace_size": ([ctypes.POINTER(_Csr), ctypes.c_int, ctypes.c_int], ctypes.c_size_t),
             "jx_jaccard_host": ([i32, i32, _VP, _VP, _VP, _VP, ctypes.c_int], ctypes.c_int),
+            "jx_jaccard_noalloc": ([ctypes.POINTER(_Csr), _VP, _VP, ctypes.c_int, _VP], ctypes.c_int),
             "jx_rowsum": ([i32, i32, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
             "jx_fill": ([i64, _VP, f32, _VP], ctypes.c_int),
             "jx_intersect": ([i32, i32, _VP, _VP, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
@@ -180,6 +181,23 @@ def jaccard(graph: GraphCSRView, weights=None, result=None, edge_centric: bool =
         _check(L.jx_jaccard_ws(ctypes.byref(g), wp, rp, algo, ctypes.c_void_p(workspace.data_ptr()),
                                workspace.numel() * workspace.element_size(), _stream(stream)),
                "jx_jaccard_ws")
+    return result
+
+
+def jaccard_noalloc(graph: GraphCSRView, weights=None, result=None, edge_centric: bool = False,
+                    stream=None):
+    """:func:`jaccard` through ``jx_jaccard_noalloc``: no device allocation inside the call
+    (graphs of at most 2**20 vertices; calls sharing the library's fixed workspace must not
+    overlap on the GPU)."""
+    torch = _torch()
+    E = graph.number_of_edges
+    if result is None:
+        result = torch.empty(E, dtype=torch.float32, device=graph.indices.device)
+    g = graph._c()
+    _check(lib().jx_jaccard_noalloc(ctypes.byref(g), _ptr(weights, torch.float32, graph.number_of_vertices, "weights"),
+                                    _ptr(result, torch.float32, E, "result"),
+                                    ALGO_EDGE_CENTRIC if edge_centric else ALGO_VERTEX_CENTRIC, _stream(stream)),
+           "jx_jaccard_noalloc")
     return result
 
 

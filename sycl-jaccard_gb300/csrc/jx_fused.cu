@@ -34,6 +34,8 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <mutex>
+#include <vector>
 
 namespace cg = cooperative_groups;
 
@@ -949,6 +951,37 @@ static jx_status dispatch(const jx_csr &g, const float *vertex_w, float *out_j, 
   return run_fused<false, false>(g, nullptr, out_j, ws, P, s);
 }
 
+// ---------------------------------------------------------------- fixed-scratch entry point
+// Workspace for jx_jaccard_noalloc: a file-scope device array, so that entry point never
+// allocates.  Every GPU that loads this library holds it until the process exits.  All
+// calls share it.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[JX_NOALLOC_SCRATCH_BYTES];
+
+// A small grid whose workspace for any graph of at most JX_NOALLOC_MAX_VERTICES vertices fits
+// the array: 8 B2 CTAs, one hub cluster, 1024 ids per class stream (overflows resume).
+static Plan noalloc_plan() { return Plan{8, 1, 1024, 1024}; }
+
+// Device address of g_noalloc_scratch on the current device.  In host code the symbol names a
+// host-side stand-in, not device memory, so the address is looked up once per device (with
+// that device current) and cached.
+static jx_status noalloc_scratch(char **ptr) {
+  static std::mutex mu;
+  static std::vector<void *> addr;
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) return set_cuda_error(ce);
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)addr.size() <= dev) addr.resize(dev + 1, nullptr);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (ce != cudaSuccess) return set_cuda_error(ce);
+    addr[dev] = p;
+  }
+  *ptr = static_cast<char *>(addr[dev]);
+  return JX_OK;
+}
+
 } // namespace jx
 
 using namespace jx;
@@ -987,6 +1020,23 @@ jx_status jx_jaccard(const jx_csr *g, const float *vertex_w, float *out_j, jx_al
   ce = cudaFreeAsync(ws, s);
   if (st != JX_OK) return st;
   return ce == cudaSuccess ? JX_OK : set_cuda_error(ce);
+}
+
+// Same operator and results as jx_jaccard, with its workspace in g_noalloc_scratch instead
+// of allocated memory.  Rejects graphs above JX_NOALLOC_MAX_VERTICES with JX_ERR_TOO_LARGE.
+jx_status jx_jaccard_noalloc(const jx_csr *g, const float *vertex_w, float *out_j, jx_algo algo,
+                             jx_stream_t stream) {
+  bool run;
+  const jx_status st0 = check_args(g, algo, out_j, &run);
+  if (!run) return st0;
+  if (g->n > JX_NOALLOC_MAX_VERTICES) return JX_ERR_TOO_LARGE;
+  const bool weighted = vertex_w != nullptr && algo == JX_ALGO_VERTEX_CENTRIC;
+  const Plan P = noalloc_plan();
+  if (layout(g->n, g->e, weighted, P).total > (size_t)JX_NOALLOC_SCRATCH_BYTES) return JX_ERR_TOO_LARGE;
+  char *ws = nullptr;
+  const jx_status st = noalloc_scratch(&ws);
+  if (st != JX_OK) return st;
+  return dispatch(*g, weighted ? vertex_w : nullptr, out_j, algo, ws, P, (cudaStream_t)stream);
 }
 
 } // extern "C"
