@@ -247,52 +247,6 @@ __device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, const 
   return acc;
 }
 
-// Weighted tasks with at most `lim` matched values wait in a per-warp batch until 32 are
-// pending; then each lane folds one task's chain, in order.  Value i of slot t is stored at
-// buf[(i / 4) * 128 + 4 * t + i % 4], so one float4 load per lane fetches 4 consecutive
-// values of every pending task (512 contiguous bytes).  The per-task metadata lives in the
-// registers of the lane that owns the slot.
-struct Batch {
-  float *buf; // 32 * lim floats of this warp
-  int lim;    // multiple of 16
-  int nb = 0, maxcnt = 0;
-  int64_t e_uv = 0, e_vu = -1;
-  int32_t du = 0, dv = 0, cnt = 0;
-  float Su = 0.0f, Sv = 0.0f;
-};
-
-// Number of matched values over all classes (counts: lane c holds class c's, others 0).
-__device__ __forceinline__ int32_t class_total(int32_t my_count) { return __reduce_add_sync(kFull, my_count); }
-
-// Gather the weights of the matched ids in class-major order into batch slot `slot`.
-template <class S>
-__device__ __forceinline__ void compact_to_batch(const S &cls, int32_t my_count, const float *__restrict__ w,
-                                                 float *buf, int slot) {
-  const int lane = threadIdx.x & 31;
-  int32_t incl = my_count;
-#pragma unroll
-  for (int o = 1; o < 8; o <<= 1) {
-    const int32_t y = __shfl_up_sync(kFull, incl, o);
-    if (lane >= o) incl += y;
-  }
-  const int32_t total = __shfl_sync(kFull, incl, 7);
-  int32_t start[8];
-#pragma unroll
-  for (int c = 0; c < 8; ++c) start[c] = __shfl_sync(kFull, incl - my_count, c);
-  for (int32_t i = lane; i < total; i += 32) {
-    int c = 0;
-    int32_t sc = 0;
-#pragma unroll
-    for (int q = 1; q < 8; ++q)
-      if (i >= start[q]) {
-        c = q;
-        sc = start[q];
-      }
-    __stcg(buf + (i >> 2) * 128 + 4 * slot + (i & 3), __ldg(w + cls.get(c, i - sc)));
-  }
-  __syncwarp();
-}
-
 using ClassStreams = Streams<true>;
 using SmemClassStreams = Streams<false>;
 
@@ -402,13 +356,10 @@ __device__ __forceinline__ void task_chunk(const Probe &probe, const int32_t *__
 // Chunked stream of N(v) = col[vs, vs+dv) through `probe`.  Returns the intersection value in
 // the reference's order (count when unweighted) and a position of u in N(v) in `mirror`
 // (-1 absent).  Counts and the position of u are kept per lane and reduced once per task.
-// kDefer: when no class overflowed, leave the values in the class streams, set `deferred`
-// and return each class's count in lane c (other lanes 0) through `my_count`.
-template <bool kWeighted, bool kDefer = false, class Probe, class Streams>
+template <bool kWeighted, class Probe, class Streams>
 __device__ __forceinline__ float task_stream(const Probe &probe, const int32_t *__restrict__ col,
                                              const float *__restrict__ w, int32_t u, int32_t vs,
-                                             int32_t dv, int32_t &mirror, const Streams &cls,
-                                             bool *deferred = nullptr, int32_t *my_count = nullptr) {
+                                             int32_t dv, int32_t &mirror, const Streams &cls) {
   const int lane = threadIdx.x & 31;
   const int my_class = lane & 7;
   int32_t cnt = 0, upos = -1;
@@ -427,11 +378,6 @@ __device__ __forceinline__ float task_stream(const Probe &probe, const int32_t *
   __syncwarp();
   float acc = 0.0f;
   if (!__any_sync(kFull, ccount > cls.cap)) {
-    if (kDefer) {
-      *deferred = true;
-      *my_count = lane < 8 ? ccount : 0;
-      return 0.0f;
-    }
     acc = fold_all(cls, lane < 8 ? ccount : 0, w, acc);
     __syncwarp();
     return acc;
@@ -598,41 +544,14 @@ __global__ void __launch_bounds__(kRowThreads) b0_kernel(
 }
 
 // ---------------------------------------------------------------- task batches
-// Fold every pending task of the batch (lane t folds slot t) and write its results.
-template <bool kEC>
-__device__ __forceinline__ void flush_batch(Batch &B, float *__restrict__ out) {
-  const int lane = threadIdx.x & 31;
-  __syncwarp();
-  if (B.nb == 0) return;
-  const bool mine = lane < B.nb;
-  float acc = 0.0f;
-  const float *p = B.buf + 4 * lane;
-  for (int32_t s = 0; s < B.maxcnt; s += 16) {
-    const float4 a = __ldcg(reinterpret_cast<const float4 *>(p + (s >> 2) * 128));
-    const float4 b = __ldcg(reinterpret_cast<const float4 *>(p + ((s >> 2) + 1) * 128));
-    const float4 c = __ldcg(reinterpret_cast<const float4 *>(p + ((s >> 2) + 2) * 128));
-    const float4 d = __ldcg(reinterpret_cast<const float4 *>(p + ((s >> 2) + 3) * 128));
-    const float v[16] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w, d.x, d.y, d.z, d.w};
-#pragma unroll
-    for (int q = 0; q < 16; ++q)
-      if (mine && s + q < B.cnt) acc = v[q] + acc;
-  }
-  if (mine) write_task<kEC, true>(acc, B.du, B.dv, B.Su, B.Sv, B.e_uv, B.e_vu, out);
-  B.nb = 0;
-  B.maxcnt = 0;
-  __syncwarp();
-}
-
 // Lanes fetch up to 32 candidate tasks (neighbours k0 .. k_end of row u) at once; the warp
-// then runs the ones with d_v <= d_u one by one.  kDefer (weighted): small tasks go to the
-// batch instead of being folded at once.
-template <bool kEC, bool kWeighted, bool kDefer = false, class Probe, class Streams>
+// then runs the ones with d_v <= d_u one by one.
+template <bool kEC, bool kWeighted, class Probe, class Streams>
 __device__ __forceinline__ void run_batch(const Probe &probe, const Streams &cls,
                                           const int32_t *__restrict__ row_ptr,
                                           const int32_t *__restrict__ col, const float *__restrict__ w,
                                           const float *__restrict__ S, int32_t u, int32_t us, int32_t du,
-                                          float Su, int32_t k0, int32_t k_end, float *__restrict__ out,
-                                          Batch *B = nullptr) {
+                                          float Su, int32_t k0, int32_t k_end, float *__restrict__ out) {
   const int lane = threadIdx.x & 31;
   int32_t v = -1, vs = 0, dv = 0;
   if (k0 + lane < k_end) {
@@ -647,40 +566,10 @@ __device__ __forceinline__ void run_batch(const Probe &probe, const Streams &cls
     const int32_t tv = __shfl_sync(kFull, v, b), tvs = __shfl_sync(kFull, vs, b),
                   tdv = __shfl_sync(kFull, dv, b);
     int32_t mirror;
-    const int64_t e_uv = (int64_t)us + k0 + b;
-    if (kDefer) {
-      bool deferred = false;
-      int32_t my_count = 0;
-      float I = task_stream<true, true>(probe, col, w, u, tvs, tdv, mirror, cls, &deferred, &my_count);
-      const int64_t e_vu = mirror >= 0 ? (int64_t)tvs + mirror : -1;
-      if (deferred) {
-        const int32_t total = class_total(my_count);
-        if (total <= B->lim) {
-          if (B->nb == 32) flush_batch<kEC>(*B, out);
-          compact_to_batch(cls, my_count, w, B->buf, B->nb);
-          if (lane == B->nb) {
-            B->e_uv = e_uv;
-            B->e_vu = e_vu;
-            B->du = du;
-            B->dv = tdv;
-            B->cnt = total;
-            B->Su = Su;
-            B->Sv = __ldg(S + tv);
-          }
-          B->nb += 1;
-          B->maxcnt = max(B->maxcnt, total);
-          continue;
-        }
-        I = fold_all(cls, my_count, w, 0.0f);
-        __syncwarp();
-      }
-      if (lane == 0) write_task<kEC, true>(I, du, tdv, Su, __ldg(S + tv), e_uv, e_vu, out);
-    } else {
-      const float I = task_stream<kWeighted>(probe, col, w, u, tvs, tdv, mirror, cls);
-      if (lane == 0)
-        write_task<kEC, kWeighted>(I, du, tdv, Su, kWeighted ? __ldg(S + tv) : 0.0f, e_uv,
-                                   mirror >= 0 ? (int64_t)tvs + mirror : -1, out);
-    }
+    const float I = task_stream<kWeighted>(probe, col, w, u, tvs, tdv, mirror, cls);
+    if (lane == 0)
+      write_task<kEC, kWeighted>(I, du, tdv, Su, kWeighted ? __ldg(S + tv) : 0.0f, (int64_t)us + k0 + b,
+                                 mirror >= 0 ? (int64_t)tvs + mirror : -1, out);
   }
 }
 
@@ -743,7 +632,7 @@ template <bool kEC, bool kWeighted, class Probe>
 __device__ __forceinline__ void b2_tasks(const Probe &probe, const ClassStreams &cls, int32_t *s_task,
                                          const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
                                          const float *__restrict__ w, const float *__restrict__ S, int32_t u,
-                                         int32_t us, int32_t du, float *__restrict__ out, Batch *B) {
+                                         int32_t us, int32_t du, float *__restrict__ out) {
   const int lane = threadIdx.x & 31;
   const float Su = kWeighted ? __ldg(S + u) : 0.0f;
   for (;;) {
@@ -751,7 +640,7 @@ __device__ __forceinline__ void b2_tasks(const Probe &probe, const ClassStreams 
     if (lane == 0) k0 = atomicAdd(s_task, 32);
     k0 = __shfl_sync(kFull, k0, 0);
     if (k0 >= du) break;
-    run_batch<kEC, kWeighted, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, du, out, B);
+    run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, du, out);
   }
 }
 
@@ -759,16 +648,11 @@ template <bool kEC, bool kWeighted>
 __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
     const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
-    float *__restrict__ out, int32_t *__restrict__ scratch, int cap, float *__restrict__ batch,
-    int batch_lim) {
+    float *__restrict__ out, int32_t *__restrict__ scratch, int cap) {
   extern __shared__ int32_t table[];
   __shared__ int32_t s_row, s_task, s_fail;
   const int wid = threadIdx.x >> 5;
-  const int64_t gw = (int64_t)blockIdx.x * (kB2Threads / 32) + wid;
-  const ClassStreams cls{scratch + gw * 8 * cap, cap};
-  Batch B;
-  B.buf = batch + gw * 32 * batch_lim;
-  B.lim = batch_lim;
+  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kB2Threads / 32) + wid) * 8 * cap, cap};
   const int32_t r0 = cnt[kOffKeys + 32], r1 = cnt[kOffKeys + 64];
   for (;;) {
     if (threadIdx.x == 0) {
@@ -796,17 +680,16 @@ __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
       if (!failed) break;
     }
     if (seed < kCuckooSeeds) {
-      b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), cls, &s_task, row_ptr, col, w, S, u, us, du, out, &B);
+      b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), cls, &s_task, row_ptr, col, w, S, u, us, du, out);
     } else { // eviction cycles with every multiplier: linear probing (load <= 0.43)
       for (uint32_t k = threadIdx.x; k < slots; k += blockDim.x) table[k] = kEmpty;
       __syncthreads();
       for (int32_t k = threadIdx.x; k < du; k += blockDim.x) hset_insert(table, slots, __ldg(col + us + k));
       __syncthreads();
-      b2_tasks<kEC, kWeighted>(HashProbe{table, slots}, cls, &s_task, row_ptr, col, w, S, u, us, du, out, &B);
+      b2_tasks<kEC, kWeighted>(HashProbe{table, slots}, cls, &s_task, row_ptr, col, w, S, u, us, du, out);
     }
     __syncthreads();
   }
-  if (kWeighted) flush_batch<kEC>(B, out);
 }
 
 // ---------------------------------------------------------------- hubs: 8-CTA clusters
@@ -819,19 +702,14 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
     const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
     const int32_t *__restrict__ unit_off, uint32_t *__restrict__ bitmaps, int64_t words,
-    float *__restrict__ out, int32_t *__restrict__ scratch, int cap, float *__restrict__ batch,
-    int batch_lim) {
+    float *__restrict__ out, int32_t *__restrict__ scratch, int cap) {
   cg::cluster_group cluster = cg::this_cluster();
   __shared__ int32_t s_unit, s_task;
   const unsigned rank = cluster.block_rank();
   const int64_t cid = blockIdx.x / kCluster;
   uint32_t *bm = bitmaps + cid * words;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int64_t gw = (int64_t)blockIdx.x * (kHubThreads / 32) + wid;
-  const ClassStreams cls{scratch + gw * 8 * cap, cap};
-  Batch B;
-  B.buf = batch + gw * 32 * batch_lim;
-  B.lim = batch_lim;
+  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kHubThreads / 32) + wid) * 8 * cap, cap};
   int32_t *unit_p = cluster.map_shared_rank(&s_unit, 0);
   int32_t *task_p = cluster.map_shared_rank(&s_task, 0);
   const int32_t h0 = cnt[kOffKeys + 0];
@@ -867,7 +745,7 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
       if (lane == 0) k0 = k_begin + atomicAdd(task_p, 32);
       k0 = __shfl_sync(kFull, k0, 0);
       if (k0 >= k_end) break;
-      run_batch<kEC, kWeighted, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, k_end, out, &B);
+      run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, k_end, out);
     }
     cluster.sync();
     for (int32_t k = rank * blockDim.x + threadIdx.x; k < du; k += kCluster * blockDim.x)
@@ -878,7 +756,6 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
     }
     cluster.sync();
   }
-  if (kWeighted) flush_batch<kEC>(B, out);
   // no CTA may exit while another can still read rank 0's shared memory
   cluster.sync();
 }
@@ -947,16 +824,15 @@ struct Plan {
   int b2_ctas;      // CTAs of the B2 kernel (one class-stream region per warp)
   int hub_clusters; // 8-CTA clusters of the hub kernel (one bitmap slot each)
   int cap_b2, cap_hub;
-  int batch_lim;    // longest chain a weighted task may park in the warp batch (multiple of 16)
 };
 
 static Plan default_plan() {
   const int sms = sm_count();
-  return Plan{sms, sms / kCluster > 0 ? sms / kCluster : 1, kCap, kHubCap, 512};
+  return Plan{sms, sms / kCluster > 0 ? sms / kCluster : 1, kCap, kHubCap};
 }
 
 struct Layout {
-  size_t cnt, rows, unit_off, S, scratch, batch, bitmaps, total;
+  size_t cnt, rows, unit_off, S, scratch, bitmaps, total;
   int64_t words;
 };
 
@@ -975,9 +851,6 @@ static Layout layout(int32_t n, int32_t e, bool weighted_vc, const Plan &P) {
   const size_t b2_ids = (size_t)P.b2_ctas * (kB2Threads / 32) * 8 * P.cap_b2;
   const size_t hub_ids = (size_t)P.hub_clusters * kCluster * (kHubThreads / 32) * 8 * P.cap_hub;
   L.scratch = off;  off += weighted_vc ? align256(sizeof(int32_t) * std::max(b2_ids, hub_ids)) : 0;
-  const size_t warps = std::max((size_t)P.b2_ctas * (kB2Threads / 32),
-                                (size_t)P.hub_clusters * kCluster * (kHubThreads / 32));
-  L.batch = off;    off += weighted_vc ? align256(sizeof(float) * warps * 32 * P.batch_lim) : 0;
   L.bitmaps = off;  off += align256(sizeof(uint32_t) * (size_t)L.words * P.hub_clusters);
   L.total = off;
   return L;
@@ -993,7 +866,6 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
   int32_t *unit_off = reinterpret_cast<int32_t *>(ws + L.unit_off);
   float *S = kWeighted ? reinterpret_cast<float *>(ws + L.S) : nullptr;
   int32_t *scratch = kWeighted ? reinterpret_cast<int32_t *>(ws + L.scratch) : nullptr;
-  float *batch = kWeighted ? reinterpret_cast<float *>(ws + L.batch) : nullptr;
   uint32_t *bitmaps = reinterpret_cast<uint32_t *>(ws + L.bitmaps);
   const int sms = sm_count();
   jx_status st;
@@ -1034,8 +906,7 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
     cfg.numAttrs = 1;
     ce = cudaLaunchKernelEx(&cfg, hub_kernel<kEC, kWeighted>, (const int32_t *)g.row_ptr,
                             (const int32_t *)g.col_idx, w, (const float *)S, (const int32_t *)rows, cnt,
-                            (const int32_t *)unit_off, bitmaps, (int64_t)L.words, out, scratch, P.cap_hub,
-                            batch, P.batch_lim);
+                            (const int32_t *)unit_off, bitmaps, (int64_t)L.words, out, scratch, P.cap_hub);
     if (ce != cudaSuccess) return set_cuda_error(ce);
     if ((st = check_launch()) != JX_OK) return st;
     prof_mark("hub_rows", s);
@@ -1044,7 +915,7 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
   ce = cudaFuncSetAttribute(b2_kernel<kEC, kWeighted>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b2);
   if (ce != cudaSuccess) return set_cuda_error(ce);
   b2_kernel<kEC, kWeighted><<<P.b2_ctas, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out,
-                                                                   scratch, P.cap_b2, batch, P.batch_lim);
+                                                                   scratch, P.cap_b2);
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("cta_rows", s);
   const size_t smem_b1 = sizeof(int32_t) * (kRowThreads / 32) * (kB1Slots + (kWeighted ? 8 * kB1Cap : 0));
@@ -1087,9 +958,8 @@ static jx_status dispatch(const jx_csr &g, const float *vertex_w, float *out_j, 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[JX_NOALLOC_SCRATCH_BYTES];
 
 // A small grid whose workspace for any graph of at most JX_NOALLOC_MAX_VERTICES vertices fits
-// the array: 8 B2 CTAs, one hub cluster, 1024 ids per class stream (overflows resume),
-// weighted chains of up to 128 values batched.
-static Plan noalloc_plan() { return Plan{8, 1, 1024, 1024, 128}; }
+// the array: 8 B2 CTAs, one hub cluster, 1024 ids per class stream (overflows resume).
+static Plan noalloc_plan() { return Plan{8, 1, 1024, 1024}; }
 
 // Device address of g_noalloc_scratch on the current device.  In host code the symbol names a
 // host-side stand-in, not device memory, so the address is looked up once per device (with
