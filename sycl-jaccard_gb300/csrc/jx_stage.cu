@@ -13,12 +13,20 @@ namespace jx {
 // A row of at most 32 elements is one chunk: one thread evaluates the 32-leaf tree itself
 // (pairs (2i+1, 2i), then pairs of pairs, ...; zeros past the end), which is the same set of
 // additions the scan performs for lane 31.  Longer rows are taken by the whole warp.
+// A warp takes 32 consecutive rows.  When they hold at most 1024 elements and none is longer
+// than 32, the warp loads their contiguous index span coalesced, gathers the weights into
+// shared memory, and each thread evaluates its own row's tree from there.  Otherwise each
+// short row is loaded by its own thread and rows longer than 32 go to the whole warp.
+constexpr int kRowSumSpan = 1024;
+
 template <bool kWeighted>
 __global__ void __launch_bounds__(256) rowsum_kernel(int32_t n, const int32_t *__restrict__ row_ptr,
                                                       const int32_t *__restrict__ ind,
                                                       const float *__restrict__ w,
                                                       float *__restrict__ work) {
+  __shared__ float span_buf[kWeighted ? 256 / 32 : 1][kWeighted ? kRowSumSpan : 1];
   const int lane = threadIdx.x & 31;
+  float *buf = span_buf[kWeighted ? (threadIdx.x >> 5) : 0];
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = base + threadIdx.x;
     int32_t start = 0, len = 0;
@@ -30,24 +38,33 @@ __global__ void __launch_bounds__(256) rowsum_kernel(int32_t n, const int32_t *_
       if (r < n) work[r] = (float)len;
       continue;
     }
+    const int32_t s0 = __shfl_sync(kFull, start, 0);
+    const int32_t last = __reduce_max_sync(kFull, r < n ? start + len : 0);
+    const bool staged = __all_sync(kFull, len <= 32) && last - s0 <= kRowSumSpan;
+    if (staged) {
+      for (int32_t i = lane; i < last - s0; i += 32) buf[i] = __ldg(w + __ldg(ind + s0 + i));
+      __syncwarp();
+    }
     if (r < n && len <= 32) {
       float x[32];
 #pragma unroll
-      for (int i = 0; i < 32; ++i) x[i] = i < len ? __ldg(w + __ldg(ind + start + i)) : 0.0f;
+      for (int i = 0; i < 32; ++i)
+        x[i] = i < len ? (staged ? buf[start - s0 + i] : __ldg(w + __ldg(ind + start + i))) : 0.0f;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1)
 #pragma unroll
         for (int i = 0; i < 32; i += 2 * o) x[i] = x[i + o] + x[i];
       work[r] = x[0] + 0.0f;
     }
+    __syncwarp();
     unsigned longs = __ballot_sync(kFull, r < n && len > 32);
     while (longs) {
       const int b = __ffs(longs) - 1;
       longs &= longs - 1;
-      const int32_t s0 = __shfl_sync(kFull, start, b), l0 = __shfl_sync(kFull, len, b);
+      const int32_t sb = __shfl_sync(kFull, start, b), lb = __shfl_sync(kFull, len, b);
       float total = 0.0f;
-      for (int32_t i0 = 0; i0 < l0; i0 += 32) {
-        const float x = (i0 + lane < l0) ? __ldg(w + __ldg(ind + s0 + i0 + lane)) : 0.0f;
+      for (int32_t i0 = 0; i0 < lb; i0 += 32) {
+        const float x = (i0 + lane < lb) ? __ldg(w + __ldg(ind + sb + i0 + lane)) : 0.0f;
         total = warp_tree_sum(x) + total;
       }
       if (lane == b) work[r] = total;
