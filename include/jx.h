@@ -159,6 +159,30 @@ jx_status jx_ec_scan(int32_t e, int32_t n, const int32_t *row_ptr, int32_t *dest
 jx_status jx_ec_unweighted(int32_t e, int32_t n, const int32_t *row_ptr, const int32_t *col_idx,
                            const int32_t *dest_ind, float *weight_j, jx_stream_t stream);
 
+/* ------------------------------------------------------------------ next to the path */
+
+/* jaccard_list (standalone_algorithms.hpp:109-133, jaccard.cpp:957-988): J for explicit pairs
+ * (first[p], second[p]), p < num_pairs, computed like the vertex-centric edge (first, second)
+ * (same ref/cur rule, same accumulation order, J = I / (S_first + S_second - I)).  The
+ * reference's pair kernel accumulates into the wrong slot (jaccard.cpp:517, 528); this is the
+ * intended result.  vertex_w NULL = unweighted.  Pair vertices must lie in [0, n).
+ * device pointers; asynchronous. */
+jx_status jx_jaccard_list(const jx_csr *g, const float *vertex_w, int64_t num_pairs,
+                          const int32_t *first, const int32_t *second, float *out,
+                          jx_stream_t stream);
+
+/* The edge-centric driver's "non zero pairs" count (jaccard.cpp:810-819): *count (device,
+ * unsigned long long) = number of values[k] > thresh (the reference uses 0.00001). */
+jx_status jx_count_above(int64_t e, const float *values, float thresh, unsigned long long *count,
+                         jx_stream_t stream);
+
+/* Reverse-edge removal of the driver's output path (main.cpp:307-309,
+ * readMtxToCSR.cpp:134-147): keeps (a,b,v) when a > b, or a < b and the reverse edge is absent
+ * or holds a different value; drops self loops.  Writes the survivors in CSR order to
+ * src/dst/out_values (device, capacity e) and their number to *count (device int64). */
+jx_status jx_remove_reverse_edges(const jx_csr *g, const float *values, int32_t *src, int32_t *dst,
+                                  float *out_values, int64_t *count, jx_stream_t stream);
+
 /* ------------------------------------------------------------------ utilities */
 
 /* Validate a CSR on the device; *flags receives JX_CSR_* bits (0 = valid, sorted, symmetric).

@@ -9,8 +9,9 @@ Builds two host libraries with gcc/g++ (no GPU, no cmake):
 
 The reference sources are read where they lie (``/root/reference``) or, on a machine without
 that directory, from the git-ignored copy in ``baseline/_ref/src`` that ``--install`` makes.
-Only the four files the hot path needs are used: jaccard.cpp, jaccard.hpp,
-standalone_algorithms.hpp, standalone_csr.hpp.
+Only the files the path and its data formats need are used: jaccard.cpp, jaccard.hpp,
+standalone_algorithms.hpp, standalone_csr.hpp, and the CSR/MTX I/O of readMtxToCSR.cpp/.hpp
+and filetypes.cpp/.hpp.
 """
 from __future__ import annotations
 
@@ -23,7 +24,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 REF_DIRS = ["/root/reference", os.path.join(ROOT, "baseline", "_ref", "src")]
-REF_FILES = ["jaccard.cpp", "jaccard.hpp", "standalone_algorithms.hpp", "standalone_csr.hpp"]
+REF_FILES = ["jaccard.cpp", "jaccard.hpp", "standalone_algorithms.hpp", "standalone_csr.hpp",
+             "readMtxToCSR.cpp", "readMtxToCSR.hpp", "filetypes.cpp", "filetypes.hpp"]
 ORACLE_SO = os.path.join(HERE, "libjxoracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libjxref.so")
 # The reference's shipped configuration (Makefile:33, Makefile:387, ICX flags Makefile:74).
@@ -73,7 +75,8 @@ def build_ref(force: bool = False) -> str | None:
     if d is None:
         return None
     os.makedirs(os.path.dirname(REF_SO), exist_ok=True)
-    srcs = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "syclshim", "syclshim.cpp")]
+    srcs = [os.path.join(HERE, "ref_driver.cpp"), os.path.join(HERE, "syclshim", "syclshim.cpp"),
+            os.path.join(d, "readMtxToCSR.cpp"), os.path.join(d, "filetypes.cpp")]
     deps = srcs + [os.path.join(HERE, "syclshim", "CL", "sycl.hpp")] + [os.path.join(d, f) for f in REF_FILES]
     if force or _stale(REF_SO, deps):
         _run(["g++", "-O3", "-std=c++20", "-fopenmp", "-fPIC", "-shared", "-w",

@@ -299,3 +299,37 @@ void jxo_jaccard_f64_rows(int32_t n, const int32_t *row_ptr, const int32_t *ind,
     }
   free(S);
 }
+
+/*
+ * jaccard_list restated with its intended semantics (standalone_algorithms.hpp:109-133,
+ * jaccard.cpp:957-988; the reference's pair kernel writes weight_i[i] instead of
+ * weight_i[idx], jaccard.cpp:517, 528): each pair (first, second) is computed like the
+ * vertex-centric edge (first, second) -- ref = shorter list, ties to second
+ * (jaccard.cpp:476-477), sum in the 8-i-lane order, J = I / (S_first + S_second - I).
+ */
+void jxo_jaccard_list(int32_t n, const int32_t *row_ptr, const int32_t *ind, const float *w,
+                      int64_t np, const int32_t *first, const int32_t *second, float *out,
+                      int nthreads) {
+  jxo_threads(nthreads);
+  float *S = (float *)malloc(sizeof(float) * (n > 0 ? n : 1));
+  if (!S) return;
+  jxo_rowsum(n, row_ptr, ind, w, S, nthreads);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t p = 0; p < np; ++p) {
+    const int32_t row = first[p], col = second[p];
+    const int32_t Ni = row_ptr[row + 1] - row_ptr[row];
+    const int32_t Nj = row_ptr[col + 1] - row_ptr[col];
+    const int32_t ref = (Ni < Nj) ? row : col;
+    const int32_t cur = (Ni < Nj) ? col : row;
+    float acc = 0.0f;
+    for (int il = 0; il < JXO_IS_I_LANES; ++il)
+      for (int32_t i = row_ptr[ref] + il; i < row_ptr[ref + 1]; i += JXO_IS_I_LANES) {
+        const int32_t ref_col = ind[i];
+        const float ref_val = w ? w[ref_col] : 1.0f;
+        if (jxo_found(ind, row_ptr[cur], row_ptr[cur + 1] - 1, ref_col)) acc = ref_val + acc;
+      }
+    const float Ws = S[row] + S[col];
+    out[p] = acc / (Ws - acc);
+  }
+  free(S);
+}

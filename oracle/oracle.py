@@ -47,6 +47,8 @@ def lib():
                                       ctypes.c_int]
         L.jxo_jaccard_f64_rows.argtypes = [ctypes.c_int32, _I32, _I32, _F32, ctypes.c_int32,
                                            ctypes.c_int32, _F64, ctypes.c_int]
+        L.jxo_jaccard_list.argtypes = [ctypes.c_int32, _I32, _I32, _F32, ctypes.c_int64, _I32, _I32,
+                                       _F32, ctypes.c_int]
         _oracle = L
     return _oracle
 
@@ -73,6 +75,14 @@ def ref_lib():
         L.jxref_weight.argtypes = [ctypes.c_int32, _F32, _F32, _F32]
         L.jxref_ec_scan.argtypes = [ctypes.c_int32, ctypes.c_int32, _I32, _I32, _F32]
         L.jxref_ec_unweighted.argtypes = [ctypes.c_int32, ctypes.c_int32, _I32, _I32, _I32, _F32]
+        L.jxref_csr_write.argtypes = [ctypes.c_char_p, ctypes.c_int32, ctypes.c_int32, _I32, _I32, _F32,
+                                      ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.jxref_csr_header.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64),
+                                       ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_uint64)]
+        L.jxref_csr_read.argtypes = [ctypes.c_char_p, _I32, _I32, _F32]
+        L.jxref_remove_reverse.argtypes = [ctypes.c_int32, ctypes.c_int32, _I32, _I32, _F32, _I32, _I32,
+                                           _F32, ctypes.c_int64]
+        L.jxref_remove_reverse.restype = ctypes.c_int64
         _ref = L
     return _ref
 
@@ -189,3 +199,45 @@ def ref_ec_unweighted(row_ptr, col, dest, weight_j):
     ref_lib().jxref_ec_unweighted(len(col), n, _p(row_ptr, _I32), _p(col, _I32), _p(dest, _I32),
                                   _p(weight_j, _F32))
     return weight_j
+
+
+def jaccard_list(row_ptr, col, first, second, w=None, threads=0):
+    n = len(row_ptr) - 1
+    first = np.ascontiguousarray(first, np.int32)
+    second = np.ascontiguousarray(second, np.int32)
+    out = np.empty(len(first), np.float32)
+    lib().jxo_jaccard_list(n, _p(row_ptr, _I32), _p(col, _I32), _p(w, _F32), len(first),
+                           _p(first, _I32), _p(second, _I32), _p(out, _F32), threads)
+    return out
+
+
+def ref_csr_write(path, row_ptr, col, w, zero_indexed=True, directed=False, reverse_edges=True):
+    rc = ref_lib().jxref_csr_write(path.encode(), len(row_ptr) - 1, len(col), _p(row_ptr, _I32),
+                                   _p(col, _I32), _p(w, _F32), int(zero_indexed), int(directed),
+                                   int(reverse_edges))
+    if rc != 0:
+        raise OSError(f"reference CSRToFile failed ({rc})")
+
+
+def ref_csr_read(path):
+    nv, ne, fl = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_uint64()
+    L = ref_lib()
+    if L.jxref_csr_header(path.encode(), ctypes.byref(nv), ctypes.byref(ne), ctypes.byref(fl)) != 0:
+        raise OSError(path)
+    rp = np.empty(nv.value + 1, np.int32)
+    col = np.empty(ne.value, np.int32)
+    w = np.empty(ne.value, np.float32) if fl.value & 1 else None
+    if L.jxref_csr_read(path.encode(), _p(rp, _I32), _p(col, _I32), _p(w, _F32)) != 0:
+        raise OSError(path)
+    return rp, col, w, fl.value
+
+
+def ref_remove_reverse(row_ptr, col, values):
+    e = len(col)
+    src = np.empty(e, np.int32)
+    dst = np.empty(e, np.int32)
+    val = np.empty(e, np.float32)
+    values = np.ascontiguousarray(values, np.float32)
+    k = ref_lib().jxref_remove_reverse(len(row_ptr) - 1, e, _p(row_ptr, _I32), _p(col, _I32),
+                                       _p(values, _F32), _p(src, _I32), _p(dst, _I32), _p(val, _F32), e)
+    return src[:k], dst[:k], val[:k]

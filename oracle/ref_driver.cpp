@@ -17,11 +17,18 @@
  *   jxref_weight         detail::Jaccard_JwKernel::invoke           (jaccard.cpp:622-653)
  *   jxref_ec_scan        detail::Jaccard_ec_scan::invoke            (jaccard.cpp:666-700)
  *   jxref_ec_unweighted  detail::Jaccard_ec_unweighted::invoke      (jaccard.cpp:745-782)
+ *   jxref_csr_write      CSRToFile<int32_t,int32_t,float>        (readMtxToCSR.cpp:285-337)
+ *   jxref_csr_read       FileToCSR                                 (readMtxToCSR.cpp:388-395)
+ *   jxref_remove_reverse CSRToMtx + removeReverseEdges             (readMtxToCSR.cpp:134-147, 211-248)
  * The edge-centric driver prints a line to std::cout (jaccard.cpp:819); it is discarded.
  */
 #include "jaccard.cpp"
 
+#include "readMtxToCSR.hpp"
+
 #include <cstdint>
+#include <cstring>
+#include <fstream>
 #include <iostream>
 #include <streambuf>
 
@@ -149,6 +156,81 @@ int jxref_ec_unweighted(int32_t e, int32_t n, const int32_t *row_ptr, const int3
   cl::sycl::buffer<float> wj(weight_j, cl::sycl::range<1>((size_t)e));
   sygraph::detail::Jaccard_ec_unweighted<int32_t, int32_t, float>::invoke(e, n, rp, ci, di, wj, q);
   return 0;
+}
+
+/* CSRToFile with weights (the reference writes its weight copy through an unallocated pointer
+ * when isWeighted is false, readMtxToCSR.cpp:295-314, so only the weighted form is usable). */
+int jxref_csr_write(const char *path, int32_t n, int32_t e, const int32_t *offsets,
+                    const int32_t *indices, const float *weights, int zero_indexed, int directed,
+                    int reverse_edges) {
+  GraphCSRView<int32_t, int32_t, float> g(wrap(offsets, (int64_t)n + 1), wrap(indices, e), wrap(weights, e),
+                                          n, e);
+  std::ofstream f(path, std::ios_base::out | std::ios_base::trunc | std::ios_base::binary);
+  if (!f) return 1;
+  CSRToFile<int32_t, int32_t, float>(f, g, zero_indexed != 0, true, directed != 0, reverse_edges != 0);
+  return f.good() ? 0 : 2;
+}
+
+/* FileToCSR: header fields and arrays (caller sizes them from jxref_csr_header). */
+int jxref_csr_header(const char *path, int64_t *nv, int64_t *ne, uint64_t *flags) {
+  std::ifstream f(path, std::ios_base::in | std::ios_base::binary);
+  if (!f) return 1;
+  CSRFileHeader h;
+  f.read(reinterpret_cast<char *>(&h), sizeof h);
+  *nv = h.numVerts;
+  *ne = h.numEdges;
+  uint64_t bits;
+  std::memcpy(&bits, &h.flags, sizeof bits);
+  *flags = bits;
+  return 0;
+}
+
+int jxref_csr_read(const char *path, int32_t *offsets, int32_t *indices, float *weights) {
+  std::ifstream f(path, std::ios_base::in | std::ios_base::binary);
+  if (!f) return 1;
+  CSRFileHeader h;
+  void *gv = FileToCSR(f, &h);
+  if (h.flags.isVertexT64 || h.flags.isEdgeT64 || h.flags.isWeightT64) return 2;
+  auto *g = static_cast<GraphCSRView<int32_t, int32_t, float> *>(gv);
+  auto o = g->offsets.get_access<cl::sycl::access::mode::read>();
+  auto ix = g->indices.get_access<cl::sycl::access::mode::read>();
+  std::memcpy(offsets, &o[0], sizeof(int32_t) * (h.numVerts + 1));
+  std::memcpy(indices, &ix[0], sizeof(int32_t) * h.numEdges);
+  if (h.flags.isWeighted && weights) {
+    auto wa = g->edge_data.get_access<cl::sycl::access::mode::read>();
+    std::memcpy(weights, &wa[0], sizeof(float) * h.numEdges);
+  }
+  delete g;
+  return 0;
+}
+
+/* The driver's result post-processing (main.cpp:307-309): CSR + per-edge values to an MTX set,
+ * then removeReverseEdges.  Writes the surviving (src, dst, value) triples (zero-based) in the
+ * set's order; returns their number, or -1 when `cap` is too small. */
+int64_t jxref_remove_reverse(int32_t n, int32_t e, const int32_t *offsets, const int32_t *indices,
+                             const float *values, int32_t *src, int32_t *dst, float *val, int64_t cap) {
+  GraphCSRView<int32_t, int32_t, float> g(wrap(offsets, (int64_t)n + 1), wrap(indices, e), wrap(values, e),
+                                          n, e);
+  std::set<std::tuple<int32_t, int32_t, float>> *m = CSRToMtx(g, true, true);
+  {
+    NullBuf nb;
+    std::streambuf *old = std::cerr.rdbuf(&nb);
+    removeReverseEdges(*m);
+    std::cerr.rdbuf(old);
+  }
+  if ((int64_t)m->size() > cap) {
+    delete m;
+    return -1;
+  }
+  int64_t k = 0;
+  for (const auto &t : *m) {
+    src[k] = std::get<0>(t) - 1;
+    dst[k] = std::get<1>(t) - 1;
+    val[k] = std::get<2>(t);
+    ++k;
+  }
+  delete m;
+  return k;
 }
 
 } /* extern "C" */

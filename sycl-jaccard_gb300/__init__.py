@@ -25,9 +25,11 @@ import os
 import numpy as np
 
 from . import build as _build
+from . import csrfile  # noqa: F401  (binary CSR files)
 from . import graphgen  # noqa: F401  (synthetic graphs)
 
-__all__ = ["GraphCSRView", "JxError", "jaccard", "jaccard_host", "jaccard_noalloc", "rowsum", "fill", "intersect",
+__all__ = ["GraphCSRView", "JxError", "jaccard", "jaccard_host", "jaccard_noalloc", "jaccard_list",
+           "count_above", "remove_reverse_edges", "csrfile", "rowsum", "fill", "intersect",
            "weight", "ec_scan", "ec_unweighted", "csr_check", "lib", "launch_count",
            "launch_count_reset", "graphgen"]
 
@@ -84,6 +86,9 @@ def lib() -> ctypes.CDLL:
             "jx_ec_scan": ([i32, i32, _VP, _VP, _VP, _VP], ctypes.c_int),
             "jx_ec_unweighted": ([i32, i32, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
             "jx_csr_check": ([ctypes.POINTER(_Csr), u32p, _VP], ctypes.c_int),
+            "jx_jaccard_list": ([ctypes.POINTER(_Csr), _VP, i64, _VP, _VP, _VP, _VP], ctypes.c_int),
+            "jx_count_above": ([i64, _VP, f32, _VP, _VP], ctypes.c_int),
+            "jx_remove_reverse_edges": ([ctypes.POINTER(_Csr), _VP, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
             "jx_status_string": ([ctypes.c_int], ctypes.c_char_p),
             "jx_version": ([], ctypes.c_int),
             "jx_last_cuda_error": ([], ctypes.c_int),
@@ -279,6 +284,50 @@ def ec_unweighted(e, n, offsets, indices, dest_ind, weight_j, stream=None):
                                   _ptr(dest_ind, torch.int32, e, "dest_ind"),
                                   _ptr(weight_j, torch.float32, e, "weight_j"), _stream(stream)),
            "jx_ec_unweighted")
+
+
+def jaccard_list(graph: GraphCSRView, first, second, weights=None, result=None, stream=None):
+    """``jaccard_list(graph, [weights,] num_pairs, first, second, result, q)``
+    (standalone_algorithms.hpp:109-133): J for the vertex pairs (first[p], second[p])."""
+    torch = _torch()
+    npairs = first.numel()
+    if result is None:
+        result = torch.empty(npairs, dtype=torch.float32, device=first.device)
+    g = graph._c()
+    _check(lib().jx_jaccard_list(ctypes.byref(g), _ptr(weights, torch.float32, graph.number_of_vertices, "weights"),
+                                 npairs, _ptr(first, torch.int32, npairs, "first"),
+                                 _ptr(second, torch.int32, npairs, "second"),
+                                 _ptr(result, torch.float32, npairs, "result"), _stream(stream)),
+           "jx_jaccard_list")
+    return result
+
+
+def count_above(values, thresh: float = 1e-5, stream=None) -> int:
+    """The edge-centric driver's count of results above `thresh` (jaccard.cpp:810-819)."""
+    torch = _torch()
+    c = torch.zeros(1, dtype=torch.int64, device=values.device)
+    _check(lib().jx_count_above(values.numel(), _ptr(values, torch.float32, values.numel(), "values"),
+                                float(thresh), ctypes.c_void_p(c.data_ptr()), _stream(stream)), "jx_count_above")
+    return int(c.item())
+
+
+def remove_reverse_edges(graph: GraphCSRView, values, stream=None):
+    """The driver's reverse-edge removal before MTX output (main.cpp:307-309): returns the
+    surviving (src, dst, value) device tensors in CSR order."""
+    torch = _torch()
+    E = graph.number_of_edges
+    dev = graph.indices.device
+    src = torch.empty(max(E, 1), dtype=torch.int32, device=dev)
+    dst = torch.empty_like(src)
+    val = torch.empty(max(E, 1), dtype=torch.float32, device=dev)
+    cnt = torch.zeros(1, dtype=torch.int64, device=dev)
+    g = graph._c()
+    _check(lib().jx_remove_reverse_edges(ctypes.byref(g), _ptr(values, torch.float32, E, "values"),
+                                         ctypes.c_void_p(src.data_ptr()), ctypes.c_void_p(dst.data_ptr()),
+                                         ctypes.c_void_p(val.data_ptr()), ctypes.c_void_p(cnt.data_ptr()),
+                                         _stream(stream)), "jx_remove_reverse_edges")
+    k = int(cnt.item())
+    return src[:k], dst[:k], val[:k]
 
 
 def csr_check(graph: GraphCSRView, stream=None) -> set:

@@ -1,7 +1,8 @@
 """Build the engine's native libraries in-tree.
 
 * ``csrc/libjx.so``       -- the CUDA engine (all ``csrc/*.cu``), sm_103a only.
-* ``csrc/gen/libjxgen.so`` -- the host synthetic-graph generator (C++/OpenMP).
+* ``csrc/gen/libjxgen.so`` -- host code: the synthetic-graph generator (C++/OpenMP) and the
+  binary CSR file reader/writer (``include/jx_io.h``).
 
 nvcc cross-compiles without a GPU, so this runs on a CPU-only build machine as well as on
 the GPU machine.  Translation units compile in parallel; the link is a single nvcc call.
@@ -75,11 +76,11 @@ def build_engine(force: bool = False, verbose: bool = False) -> str:
 
 
 def build_generator(force: bool = False) -> str:
-    src = os.path.join(CSRC, "gen", "jxgen.cpp")
-    deps = [src, os.path.join(CSRC, "jx_rng.h")]
+    srcs = [os.path.join(CSRC, "gen", "jxgen.cpp"), os.path.join(CSRC, "gen", "jxio.cpp")]
+    deps = srcs + [os.path.join(CSRC, "jx_rng.h"), os.path.join(ROOT, "include", "jx_io.h")]
     if force or _stale(LIBGEN, deps):
         tmp = LIBGEN + ".tmp"
-        _run(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-o", tmp, src])
+        _run(["g++", "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", "-o", tmp, *srcs])
         os.replace(tmp, LIBGEN)
     return LIBGEN
 

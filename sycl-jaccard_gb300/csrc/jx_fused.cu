@@ -815,6 +815,37 @@ __global__ void __launch_bounds__(256) fixup_kernel(int32_t n, int64_t e, const 
   }
 }
 
+// ---------------------------------------------------------------- pair list
+// jaccard_list (standalone_algorithms.hpp:109-133, jaccard.cpp:957-988): J for explicit vertex
+// pairs (first[p], second[p]).  The pair is treated like the edge (first, second) of the
+// vertex-centric path: the shorter list is ref (ties: second), the sum is taken in the
+// 8-i-lane order, J = I / (S_first + S_second - I).  The reference's pair kernel
+// (Jaccard_IsPairsKernel, jaccard.cpp:462-540) accumulates into weight_i[i], the ref position,
+// instead of weight_i[idx] (jaccard.cpp:517, 528), so its results are not usable; this is the
+// intended computation.  One warp per pair; vertices must lie in [0, n).
+template <bool kWeighted>
+__global__ void __launch_bounds__(256) pairs_kernel(int64_t np, const int32_t *__restrict__ row_ptr,
+                                                    const int32_t *__restrict__ col, const float *__restrict__ w,
+                                                    const float *__restrict__ S, const int32_t *__restrict__ first,
+                                                    const int32_t *__restrict__ second, float *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < np; p += nwarps) {
+    const int32_t a = __ldg(first + p), b = __ldg(second + p);
+    const int32_t as = __ldg(row_ptr + a), Ni = __ldg(row_ptr + a + 1) - as;
+    const int32_t bs = __ldg(row_ptr + b), Nj = __ldg(row_ptr + b + 1) - bs;
+    const bool a_is_ref = Ni < Nj; // jaccard.cpp:476-477
+    const int32_t rs = a_is_ref ? as : bs, rl = a_is_ref ? Ni : Nj;
+    const int32_t cs = a_is_ref ? bs : as, cl = a_is_ref ? Nj : Ni;
+    int32_t dummy;
+    const float I = task_strided<kWeighted>(SearchProbe{col, cs, cs + cl - 1}, col, w, -1, rs, rl, dummy);
+    if (lane == 0) {
+      const float Ws = kWeighted ? (__ldg(S + a) + __ldg(S + b)) : ((float)Ni + (float)Nj); // jaccard.cpp:480
+      out[p] = I / (Ws - I);
+    }
+  }
+}
+
 // ---------------------------------------------------------------- host driver
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -1037,6 +1068,30 @@ jx_status jx_jaccard_noalloc(const jx_csr *g, const float *vertex_w, float *out_
   const jx_status st = noalloc_scratch(&ws);
   if (st != JX_OK) return st;
   return dispatch(*g, weighted ? vertex_w : nullptr, out_j, algo, ws, P, (cudaStream_t)stream);
+}
+
+jx_status jx_jaccard_list(const jx_csr *g, const float *vertex_w, int64_t num_pairs, const int32_t *first,
+                          const int32_t *second, float *out, jx_stream_t stream) {
+  if (!g || g->n < 0 || g->e < 0 || num_pairs < 0) return JX_ERR_INVALID;
+  if (num_pairs == 0) return JX_OK;
+  if (!g->row_ptr || (g->e > 0 && !g->col_idx) || !first || !second || !out) return JX_ERR_INVALID;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int64_t want = (num_pairs * 32 + 255) / 256;
+  const int grid = (int)(want < (int64_t)sm_count() * 16 ? want : (int64_t)sm_count() * 16);
+  if (!vertex_w) {
+    pairs_kernel<false><<<grid, 256, 0, s>>>(num_pairs, g->row_ptr, g->col_idx, nullptr, nullptr, first, second, out);
+    return check_launch();
+  }
+  float *S = nullptr;
+  cudaError_t ce = cudaMallocAsync(&S, sizeof(float) * ((size_t)g->n + 1), s);
+  if (ce != cudaSuccess) return set_cuda_error(ce);
+  jx_status st = jx_rowsum(g->n, g->e, g->row_ptr, g->col_idx, vertex_w, S, stream);
+  if (st == JX_OK) {
+    pairs_kernel<true><<<grid, 256, 0, s>>>(num_pairs, g->row_ptr, g->col_idx, vertex_w, S, first, second, out);
+    st = check_launch();
+  }
+  cudaFreeAsync(S, s);
+  return st;
 }
 
 } // extern "C"

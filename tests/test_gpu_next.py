@@ -1,0 +1,63 @@
+"""GPU: the operators next to the path -- pair-list Jaccard, the driver's non-zero count and
+its reverse-edge removal -- against the oracle and the reference's own post-processing."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+@pytest.fixture(scope="module")
+def g14(jx):
+    rp, col = jx.graphgen.rmat(14, 16, seed=51)
+    w = jx.graphgen.uniform_weights(len(rp) - 1, seed=52)
+    return rp, col, w
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_pair_list(jx, O, g14, weighted):
+    import torch
+    rp, col, w = g14
+    n = len(rp) - 1
+    rng = np.random.default_rng(7)
+    src = np.repeat(np.arange(n, dtype=np.int32), np.diff(rp))
+    # a mix of stored edges, random (mostly non-adjacent) pairs, self pairs and isolated vertices
+    pick = rng.integers(0, len(col), 4000)
+    first = np.concatenate([src[pick], rng.integers(0, n, 4000).astype(np.int32), np.arange(50, dtype=np.int32)])
+    second = np.concatenate([col[pick], rng.integers(0, n, 4000).astype(np.int32), np.arange(50, dtype=np.int32)])
+    ww = w if weighted else None
+    want = O.jaccard_list(rp, col, first, second, ww)
+    g = jx.GraphCSRView.from_numpy(rp, col)
+    got = jx.jaccard_list(g, torch.from_numpy(first).cuda(), torch.from_numpy(second).cuda(),
+                          None if ww is None else torch.from_numpy(ww).cuda()).cpu().numpy()
+    assert np.array_equal(bits(got), bits(want))
+    # stored edges: equal to the all-edges operator
+    allJ = jx.jaccard(g, None if ww is None else torch.from_numpy(ww).cuda()).cpu().numpy()
+    assert np.array_equal(bits(got[:4000]), bits(allJ[pick]))
+
+
+def test_count_above(jx, g14):
+    import torch
+    rp, col, w = g14
+    g = jx.GraphCSRView.from_numpy(rp, col)
+    J = jx.jaccard(g, edge_centric=True)
+    Jh = J.cpu().numpy()
+    assert jx.count_above(J, 1e-5) == int((Jh > np.float32(1e-5)).sum())
+    assert jx.count_above(J, 2.0) == 0
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_remove_reverse_edges(jx, O, g14, weighted):
+    import torch
+    if O.ref_lib() is None:
+        pytest.skip("reference sources unavailable")
+    rp, col, w = g14
+    g = jx.GraphCSRView.from_numpy(rp, col)
+    J = jx.jaccard(g, torch.from_numpy(w).cuda() if weighted else None)
+    src, dst, val = jx.remove_reverse_edges(g, J)
+    a, b, c = O.ref_remove_reverse(rp, col, J.cpu().numpy())
+    assert np.array_equal(src.cpu().numpy(), a) and np.array_equal(dst.cpu().numpy(), b)
+    assert np.array_equal(bits(val.cpu().numpy()), bits(c))
