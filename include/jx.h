@@ -183,6 +183,37 @@ jx_status jx_count_above(int64_t e, const float *values, float thresh, unsigned 
 jx_status jx_remove_reverse_edges(const jx_csr *g, const float *values, int32_t *src, int32_t *dst,
                                   float *out_values, int64_t *count, jx_stream_t stream);
 
+/* ------------------------------------------------------------------ batched mode
+ * Many graphs packed into one offset-indexed super-CSR on the device (graph g's vertex ids
+ * shifted by the vertices before it, its edges by the edges before it; at most 2^31 - 1
+ * edges and vertices in total, larger batches are split by the caller).  The graphs are
+ * disjoint components, so one operator pass over the super-CSR gives each graph its own
+ * results as a contiguous slice.  The pass is captured once as a CUDA graph and replayed by
+ * jx_batch_run.  tune != 0 times a few grid-size plans for the degree bins on the batch and
+ * keeps the fastest.  (Batching is this library's addition; the reference scores one graph
+ * per call.) */
+typedef struct {
+  int32_t n, e;
+  const int32_t *row_ptr; /* host, n + 1 */
+  const int32_t *col_idx; /* host, e */
+  const float *vertex_w;  /* host, n; required when the batch is weighted */
+} jx_host_graph;
+
+typedef struct jx_batch_s *jx_batch;
+
+/* Copies the graphs to the device (synchronous; the host arrays may be freed afterwards). */
+jx_status jx_batch_create(const jx_host_graph *graphs, int32_t ngraphs, jx_algo algo, int weighted,
+                          int tune, jx_batch *out);
+/* One pass over every graph of the batch (asynchronous on `stream`). */
+jx_status jx_batch_run(jx_batch b, jx_stream_t stream);
+/* Device slice of graph g's results (valid until destroy). */
+jx_status jx_batch_result(jx_batch b, int32_t g, const float **device_out, int64_t *count);
+/* Copy graph g's results to host memory (synchronous on `stream`). */
+jx_status jx_batch_download(jx_batch b, int32_t g, float *host_out, jx_stream_t stream);
+jx_status jx_batch_info(jx_batch b, int64_t *vertices, int64_t *edges, uint64_t *kernels_per_run,
+                        char *plan_desc, size_t len);
+void jx_batch_destroy(jx_batch b);
+
 /* ------------------------------------------------------------------ utilities */
 
 /* Validate a CSR on the device; *flags receives JX_CSR_* bits (0 = valid, sorted, symmetric).

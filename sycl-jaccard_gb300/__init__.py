@@ -29,7 +29,7 @@ from . import csrfile  # noqa: F401  (binary CSR files)
 from . import graphgen  # noqa: F401  (synthetic graphs)
 
 __all__ = ["GraphCSRView", "JxError", "jaccard", "jaccard_host", "jaccard_noalloc", "jaccard_list",
-           "count_above", "remove_reverse_edges", "csrfile", "rowsum", "fill", "intersect",
+           "count_above", "remove_reverse_edges", "csrfile", "Batch", "rowsum", "fill", "intersect",
            "weight", "ec_scan", "ec_unweighted", "csr_check", "lib", "launch_count",
            "launch_count_reset", "graphgen"]
 
@@ -50,6 +50,11 @@ class JxError(RuntimeError):
         if status == 2 and _lib is not None:
             msg += f", cudaError {_lib.jx_last_cuda_error()}"
         super().__init__(msg)
+
+
+class _HostGraph(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("e", ctypes.c_int32), ("row_ptr", ctypes.c_void_p),
+                ("col_idx", ctypes.c_void_p), ("vertex_w", ctypes.c_void_p)]
 
 
 class _Csr(ctypes.Structure):
@@ -89,6 +94,14 @@ def lib() -> ctypes.CDLL:
             "jx_jaccard_list": ([ctypes.POINTER(_Csr), _VP, i64, _VP, _VP, _VP, _VP], ctypes.c_int),
             "jx_count_above": ([i64, _VP, f32, _VP, _VP], ctypes.c_int),
             "jx_remove_reverse_edges": ([ctypes.POINTER(_Csr), _VP, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
+            "jx_batch_create": ([ctypes.POINTER(_HostGraph), i32, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                 ctypes.POINTER(_VP)], ctypes.c_int),
+            "jx_batch_run": ([_VP, _VP], ctypes.c_int),
+            "jx_batch_result": ([_VP, i32, ctypes.POINTER(_VP), ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+            "jx_batch_download": ([_VP, i32, _VP, _VP], ctypes.c_int),
+            "jx_batch_info": ([_VP, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                               ctypes.POINTER(ctypes.c_uint64), ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+            "jx_batch_destroy": ([_VP], None),
             "jx_status_string": ([ctypes.c_int], ctypes.c_char_p),
             "jx_version": ([], ctypes.c_int),
             "jx_last_cuda_error": ([], ctypes.c_int),
@@ -328,6 +341,60 @@ def remove_reverse_edges(graph: GraphCSRView, values, stream=None):
                                          _stream(stream)), "jx_remove_reverse_edges")
     k = int(cnt.item())
     return src[:k], dst[:k], val[:k]
+
+
+class Batch:
+    """Batched mode (``jx_batch_*``): host CSRs packed into one device super-CSR, one replayed
+    CUDA graph per pass over all graphs.  ``graphs``: list of (row_ptr, col_idx[, weights])
+    numpy arrays."""
+
+    def __init__(self, graphs, edge_centric: bool = False, weighted: bool = False, tune: bool = False):
+        keep = []
+        arr = (_HostGraph * len(graphs))()
+        for i, gr in enumerate(graphs):
+            rp = np.ascontiguousarray(gr[0], np.int32)
+            col = np.ascontiguousarray(gr[1], np.int32)
+            w = np.ascontiguousarray(gr[2], np.float32) if weighted else None
+            keep.append((rp, col, w))
+            arr[i] = _HostGraph(len(rp) - 1, len(col), rp.ctypes.data, col.ctypes.data,
+                                None if w is None else w.ctypes.data)
+        self._h = ctypes.c_void_p()
+        self.ngraphs = len(graphs)
+        self.edges = [len(k[1]) for k in keep]
+        _check(lib().jx_batch_create(arr, len(graphs), ALGO_EDGE_CENTRIC if edge_centric else ALGO_VERTEX_CENTRIC,
+                                     int(weighted), int(tune), ctypes.byref(self._h)), "jx_batch_create")
+
+    def run(self, stream=None):
+        _check(lib().jx_batch_run(self._h, _stream(stream)), "jx_batch_run")
+
+    def result(self, g):
+        """Device pointer and length of graph g's results."""
+        p, n = ctypes.c_void_p(), ctypes.c_int64()
+        _check(lib().jx_batch_result(self._h, g, ctypes.byref(p), ctypes.byref(n)), "jx_batch_result")
+        return p.value, n.value
+
+    def download(self, g) -> np.ndarray:
+        out = np.empty(self.edges[g], np.float32)
+        _check(lib().jx_batch_download(self._h, g, out.ctypes.data, _stream(None)), "jx_batch_download")
+        return out
+
+    def info(self) -> dict:
+        nv, ne, k = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_uint64()
+        buf = ctypes.create_string_buffer(256)
+        _check(lib().jx_batch_info(self._h, ctypes.byref(nv), ctypes.byref(ne), ctypes.byref(k), buf, 256),
+               "jx_batch_info")
+        return {"vertices": nv.value, "edges": ne.value, "kernels_per_run": k.value, "plan": buf.value.decode()}
+
+    def close(self):
+        if self._h:
+            lib().jx_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def csr_check(graph: GraphCSRView, stream=None) -> set:

@@ -30,6 +30,7 @@
 // ends one lane folds them class by class.  A class that outgrows its stream resumes with a
 // strided walk over its remaining positions (same order).
 #include "jx_common.cuh"
+#include "jx_plan.h"
 
 #include <cooperative_groups.h>
 
@@ -851,15 +852,9 @@ static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Grid sizes and class-stream capacities of one operator call.  The default plan fills the
 // GPU; the fixed-scratch entry point uses a small plan whose workspace fits its array.
-struct Plan {
-  int b2_ctas;      // CTAs of the B2 kernel (one class-stream region per warp)
-  int hub_clusters; // 8-CTA clusters of the hub kernel (one bitmap slot each)
-  int cap_b2, cap_hub;
-};
-
-static Plan default_plan() {
+Plan default_plan() {
   const int sms = sm_count();
-  return Plan{sms, sms / kCluster > 0 ? sms / kCluster : 1, kCap, kHubCap};
+  return Plan{sms, sms / kCluster > 0 ? sms / kCluster : 1, kCap, kHubCap, sms * 3, sms * 8};
 }
 
 struct Layout {
@@ -952,10 +947,10 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
   const size_t smem_b1 = sizeof(int32_t) * (kRowThreads / 32) * (kB1Slots + (kWeighted ? 8 * kB1Cap : 0));
   ce = cudaFuncSetAttribute(b1_kernel<kEC, kWeighted>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b1);
   if (ce != cudaSuccess) return set_cuda_error(ce);
-  b1_kernel<kEC, kWeighted><<<sms * 3, kRowThreads, smem_b1, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
+  b1_kernel<kEC, kWeighted><<<P.b1_ctas, kRowThreads, smem_b1, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("warp_rows", s);
-  b0_kernel<kEC, kWeighted><<<sms * 8, kRowThreads, 0, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
+  b0_kernel<kEC, kWeighted><<<P.b0_ctas, kRowThreads, 0, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("lane_rows", s);
   fixup_kernel<kEC, kWeighted><<<sms * 8, 256, 0, s>>>(n, g.e, g.row_ptr, g.col_idx, w, S, out);
@@ -982,6 +977,20 @@ static jx_status dispatch(const jx_csr &g, const float *vertex_w, float *out_j, 
   return run_fused<false, false>(g, nullptr, out_j, ws, P, s);
 }
 
+size_t plan_workspace(int32_t n, int32_t e, bool weighted_vc, const Plan &P) {
+  return layout(n, e, weighted_vc, P).total;
+}
+
+jx_status run_plan(const jx_csr &g, const float *vertex_w, float *out, jx_algo algo, void *workspace,
+                   const Plan &P, cudaStream_t s) {
+  bool run;
+  const jx_status st = check_args(&g, algo, out, &run);
+  if (!run) return st;
+  if (!workspace || (reinterpret_cast<uintptr_t>(workspace) & 255u)) return JX_ERR_INVALID;
+  const bool weighted = vertex_w != nullptr && algo == JX_ALGO_VERTEX_CENTRIC;
+  return dispatch(g, weighted ? vertex_w : nullptr, out, algo, static_cast<char *>(workspace), P, s);
+}
+
 // ---------------------------------------------------------------- fixed-scratch entry point
 // Workspace for jx_jaccard_noalloc: a file-scope device array, so that entry point never
 // allocates.  Every GPU that loads this library holds it until the process exits.  All
@@ -990,7 +999,10 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[JX_NOALLOC_SCRA
 
 // A small grid whose workspace for any graph of at most JX_NOALLOC_MAX_VERTICES vertices fits
 // the array: 8 B2 CTAs, one hub cluster, 1024 ids per class stream (overflows resume).
-static Plan noalloc_plan() { return Plan{8, 1, 1024, 1024}; }
+static Plan noalloc_plan() {
+  const int sms = sm_count();
+  return Plan{8, 1, 1024, 1024, sms * 3, sms * 8};
+}
 
 // Device address of g_noalloc_scratch on the current device.  In host code the symbol names a
 // host-side stand-in, not device memory, so the address is looked up once per device (with
