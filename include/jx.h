@@ -208,7 +208,8 @@ jx_status jx_batch_create(const jx_host_graph *graphs, int32_t ngraphs, jx_algo 
 jx_status jx_batch_run(jx_batch b, jx_stream_t stream);
 /* Device slice of graph g's results (valid until destroy). */
 jx_status jx_batch_result(jx_batch b, int32_t g, const float **device_out, int64_t *count);
-/* Copy graph g's results to host memory (synchronous on `stream`). */
+/* Copy graph g's results to host memory (synchronous on `stream`); g = -1 copies the results
+ * of every graph, concatenated in batch order (the whole super-CSR output). */
 jx_status jx_batch_download(jx_batch b, int32_t g, float *host_out, jx_stream_t stream);
 jx_status jx_batch_info(jx_batch b, int64_t *vertices, int64_t *edges, uint64_t *kernels_per_run,
                         char *plan_desc, size_t len);

@@ -373,9 +373,11 @@ class Batch:
         _check(lib().jx_batch_result(self._h, g, ctypes.byref(p), ctypes.byref(n)), "jx_batch_result")
         return p.value, n.value
 
-    def download(self, g) -> np.ndarray:
-        out = np.empty(self.edges[g], np.float32)
-        _check(lib().jx_batch_download(self._h, g, out.ctypes.data, _stream(None)), "jx_batch_download")
+    def download(self, g, out=None, stream=None) -> np.ndarray:
+        """Graph g's results on the host (g = -1: every graph's, concatenated)."""
+        if out is None:
+            out = np.empty(sum(self.edges) if g < 0 else self.edges[g], np.float32)
+        _check(lib().jx_batch_download(self._h, g, out.ctypes.data, _stream(stream)), "jx_batch_download")
         return out
 
     def info(self) -> dict:

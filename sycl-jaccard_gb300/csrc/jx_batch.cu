@@ -244,11 +244,12 @@ jx_status jx_batch_result(jx_batch b, int32_t g, const float **device_out, int64
 }
 
 jx_status jx_batch_download(jx_batch b, int32_t g, float *host_out, jx_stream_t stream) {
-  if (!b || g < 0 || g >= b->ngraphs || !host_out) return JX_ERR_INVALID;
-  const int64_t cnt = b->ebase[g + 1] - b->ebase[g];
+  if (!b || g < -1 || g >= b->ngraphs || !host_out) return JX_ERR_INVALID;
+  const int64_t first = g < 0 ? 0 : b->ebase[g];
+  const int64_t cnt = g < 0 ? b->ne : b->ebase[g + 1] - b->ebase[g];
   if (cnt == 0) return JX_OK;
   cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t ce = cudaMemcpyAsync(host_out, b->out + b->ebase[g], sizeof(float) * (size_t)cnt,
+  cudaError_t ce = cudaMemcpyAsync(host_out, b->out + first, sizeof(float) * (size_t)cnt,
                                    cudaMemcpyDeviceToHost, s);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
   return ce == cudaSuccess ? JX_OK : set_cuda_error(ce);

@@ -108,3 +108,28 @@ def config_graph(name: str, threads: int = 0):
         w = uniform_weights(len(rp) - 1, seed=4, threads=threads)
         return rp, col, w, "RMAT scale 24 ef 16 (.57,.19,.19,.05) seed 3, vertex weights U(0,1] seed 4"
     raise KeyError(name)
+
+
+def batch_graphs(count: int = 2000, seed: int = 5, threads: int = 0, vmin: int = 256, vmax: int = 262144):
+    """The batched workload: `count` graphs, vertex counts log-uniform in [vmin, vmax], half
+    Erdos-Renyi (G(n, m) with m = n * avg_degree / 2, avg degree uniform in [4, 64]) and half
+    R-MAT (scale round(log2 n), edge factor uniform in [8, 32], a = .57, b = c = .19), each
+    symmetrised / deduplicated / sorted int32 CSR.  Graph i uses seed `seed * 1000003 + i`.
+    Returns a list of (row_ptr, col_idx, description)."""
+    rng = np.random.default_rng(seed)
+    nv = np.exp(rng.uniform(np.log(vmin), np.log(vmax), count)).round().astype(np.int64)
+    kind = rng.permutation(np.arange(count) % 2)  # 0 = ER, 1 = RMAT, half each
+    deg = rng.uniform(4.0, 64.0, count)
+    ef = rng.integers(8, 33, count)
+    out = []
+    for i in range(count):
+        s = seed * 1000003 + i
+        if kind[i] == 0:
+            n = int(nv[i])
+            rp, col = er_gnm(n, int(round(n * deg[i] / 2)), seed=s, threads=threads)
+            out.append((rp, col, f"ER n={n} deg={deg[i]:.1f}"))
+        else:
+            sc = int(np.clip(np.round(np.log2(nv[i])), 8, 18))
+            rp, col = rmat(sc, int(ef[i]), 0.57, 0.19, 0.19, seed=s, threads=threads)
+            out.append((rp, col, f"RMAT scale={sc} ef={int(ef[i])}"))
+    return out
