@@ -277,22 +277,24 @@ def super_batches(st):
     return groups
 
 
-def cpu_reference_batch(graphs, st, target_s=20.0):
-    """Reference on the host cores over a stratified sample of the batch: 8 graphs evenly
-    spaced in edge-count order, each timed with cpu_reference's work-group sampling; the batch
-    rate is (sum of their edges) / (sum of their extrapolated call times)."""
+def cpu_reference_batch(graphs, st, target_s=20.0, weights=None, what="graphs of the batch"):
+    """Reference on the host cores over a stratified sample of a list of graphs: 8 graphs
+    evenly spaced in edge-count order, each timed with cpu_reference's work-group sampling; the
+    rate is (sum of their edges) / (sum of their extrapolated call times).  weights: per-graph
+    vertex weights (weighted VC) or None (unweighted VC)."""
     order = np.argsort([x["E"] for x in st], kind="stable")
     pick = [int(order[int(q)]) for q in np.linspace(0, len(order) - 1, 8)]
     E = T = 0.0
     threads, kind = None, None
     for i in pick:
-        rp, col, _ = graphs[i]
-        cb = cpu_reference(rp, col, None, target_s / len(pick))
+        rp, col = graphs[i][0], graphs[i][1]
+        cb = cpu_reference(rp, col, None if weights is None else weights[i], target_s / len(pick))
         E += st[i]["E"]
         T += cb["extrapolated_call_s"]
         threads, kind = cb["cores"], cb["kind"]
     return {"value": E / T, "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": f"reference jaccard.cpp (VC) on 8 graphs of the batch evenly spaced in edge count "
+            "sample": f"reference jaccard.cpp (VC{' weighted' if weights is not None else ''}) on 8 {what} "
+                      f"evenly spaced in edge count "
                       f"({int(E)} edges), each on a work-group sample extrapolated to its whole call; "
                       f"rate = sum of edges / sum of call times",
             "extrapolated_call_s": round(T, 3)}
@@ -420,6 +422,184 @@ def run_gpu_batched(args, world, rank, local):
     return result
 
 
+# ------------------------------------------------------------------ served workload
+
+def make_served(threads):
+    jx = importlib.import_module("sycl-jaccard_gb300")
+    t = time.time()
+    res, up = jx.graphgen.served_pools(seed=6, threads=threads)
+    st_res = [jx.graphgen.stats(g[0], g[1]) for g in res]
+    st_up = [jx.graphgen.stats(g[0], g[1]) for g in up]
+    log(f"served pools: {len(res)} resident (E={sum(x['E'] for x in st_res)}), {len(up)} uploads "
+        f"(E={sum(x['E'] for x in st_up)}) ({time.time() - t:.1f}s)")
+    return res, up, st_res, st_up
+
+
+def replay(jx, srv, trace_t, trace_g, targets, edges, alone, max_outstanding):
+    """Submit the trace at its arrival times (scheduled time = arrival stamp) and verify every
+    result against the request's graph scored alone.  At most max_outstanding requests hold a
+    result buffer at once (submission blocks beyond that; latency still counts from the
+    scheduled arrival).  Returns (mismatches, per-request latencies in ms)."""
+    import queue as q
+    done = q.Queue()
+    tickets = q.Queue()
+    sem = threading.Semaphore(max_outstanding)
+    bad = []
+
+    def collector():
+        while True:
+            item = tickets.get()
+            if item is None:
+                break
+            t, key, out = item
+            try:
+                lat = srv.wait(t)
+                if not np.array_equal(out.view(np.uint32), alone[key].view(np.uint32)):
+                    bad.append(key)
+                done.put(lat)
+            except Exception as exc:  # a failed request is a mismatch
+                bad.append((key, str(exc)))
+            finally:
+                sem.release()
+
+    th = threading.Thread(target=collector, daemon=True)
+    th.start()
+    t0 = srv.clock_ns() + 2_000_000  # 2 ms to spare before the first arrival
+    for at, key in zip(trace_t, trace_g):
+        due = t0 + int(at * 1e9)
+        while True:
+            dt = (due - srv.clock_ns()) * 1e-9
+            if dt <= 0:
+                break
+            time.sleep(dt - 50e-6 if dt > 100e-6 else 0)
+        sem.acquire()
+        out = np.empty(edges[key], np.float32)
+        tickets.put((srv.submit(targets[key], out, weighted=True, arrival_ns=due), key, out))
+    tickets.put(None)
+    th.join()
+    lats = []
+    while not done.empty():
+        lats.append(done.get())
+    return bad, lats
+
+
+def run_gpu_served(args, world, rank, local):
+    import torch
+    jx = importlib.import_module("sycl-jaccard_gb300")
+    torch.cuda.set_device(local)
+    threads = os.cpu_count() or 1
+    res, up, st_res, st_up = make_served(threads)
+    trace_t, trace_g = jx.graphgen.poisson_trace(args.requests, args.rate, len(res), len(up), seed=6)
+    # pinned host copies of the upload pool (both arms upload from them)
+    up_pinned = [tuple(torch.from_numpy(a).pin_memory().numpy() for a in g[:3]) for g in up]
+    srv = jx.Server(memory_budget=60 << 30, slots=args.slots, fold_edges=args.fold_edges,
+                    fold_max_edges=64 << 20)
+    ids = [srv.add_graph(g[0], g[1], g[2]) for g in res]
+    targets = {("resident", k): ids[k] for k in range(len(res))}
+    targets.update({("upload", k): up_pinned[k] for k in range(len(up))})
+    edges = {("resident", k): st_res[k]["E"] for k in range(len(res))}
+    edges.update({("upload", k): st_up[k]["E"] for k in range(len(up))})
+    stats = {("resident", k): st_res[k] for k in range(len(res))}
+    stats.update({("upload", k): st_up[k] for k in range(len(up))})
+
+    # alone: every graph of the pools scored by itself with the plain operator (the oracle of
+    # "same result alone and in the mix"); the same plain calls time the serial baseline
+    dev_res = [(jx.GraphCSRView.from_numpy(g[0], g[1], device=f"cuda:{local}"), torch.from_numpy(g[2]).cuda())
+               for g in res]
+    L = jx.lib()
+
+    def plain(key, out):
+        kind, k = key
+        if kind == "resident":
+            view, w = dev_res[k]
+            r = jx.jaccard(view, w)
+            torch.cuda.synchronize()
+            out[:] = r.cpu().numpy()
+        else:
+            rp, col, w = up_pinned[k]
+            rc = L.jx_jaccard_host(len(rp) - 1, len(col), rp.ctypes.data, col.ctypes.data, w.ctypes.data,
+                                   out.ctypes.data, 0)
+            assert rc == 0, rc
+
+    alone = {}
+    for key in edges:
+        alone[key] = np.empty(edges[key], np.float32)
+        plain(key, alone[key])
+
+    # serial plain launches over the same request sequence, back to back
+    torch.cuda.synchronize()
+    svc = []
+    scratch = {}
+    tp0 = time.perf_counter()
+    for key in trace_g:
+        a = time.perf_counter()
+        out = scratch.setdefault(key, np.empty(edges[key], np.float32))
+        plain(key, out)
+        svc.append(time.perf_counter() - a)
+    plain_s = time.perf_counter() - tp0
+    E_trace = sum(edges[k] for k in trace_g)
+    # the serial server's latencies under the same arrivals (queue of one, measured service times)
+    fin, plat = 0.0, []
+    for at, sv in zip(trace_t, svc):
+        fin = max(fin, at) + sv
+        plat.append((fin - at) * 1e3)
+    plat.sort()
+
+    # warm-up requests, then the timed replay
+    for i in range(args.warmup):
+        key = trace_g[i % len(trace_g)]
+        srv.wait(srv.submit(targets[key], np.empty(edges[key], np.float32), weighted=True))
+    srv.reset_stats()
+    with ClockSampler(local) as clk:
+        bad, lats = replay(jx, srv, trace_t, trace_g, targets, edges, alone, args.max_outstanding)
+    st = srv.stats()
+    clocks = clk.summary()
+    if bad or st["failed"]:
+        raise AssertionError(f"served results differ from the graphs scored alone: {bad[:5]}")
+    span = st["span_s"]
+    value = st["edges"] / span
+    B = sum(byte_model(stats[k]["V"], stats[k]["E"], stats[k]["sum_min"], True) for k in trace_g)
+    peak, peak_kind = hbm_peak()
+    achieved = B / span / 1e9
+    h2d = sum(4 * (stats[k]["V"] + 1) + 4 * stats[k]["E"] + 4 * stats[k]["V"] for k in trace_g if k[0] == "upload")
+    result = {
+        "metric": METRIC, "value": value * world, "unit": UNIT, "n_gpus": world, "steps": 1,
+        "warmup": args.warmup, "ms_per_step": round(span * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"served: {args.requests} requests, Poisson {args.rate:g}/s seed 6; 70% all edges "
+                               f"of a resident graph (64 RMAT scale 14-20 ef 16), 30% uploads (32-graph pool, "
+                               f"ER/RMAT 1e3-1e6 vertices); weighted VC, weights U(0,1]; budget 60 GB",
+                   "slots": args.slots, "fold_edges": args.fold_edges, "E_trace": E_trace,
+                   "l2": "graphs up to 1.3 GB; consecutive requests mostly touch different graphs; no flush",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "served": {"p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                   "mean_ms": round(st["mean_ms"], 3), "max_ms": round(st["max_ms"], 3),
+                   "completed": st["completed"], "passes": st["passes"],
+                   "folded_requests": st["folded_requests"],
+                   "peak_device_bytes": st["peak_reserved"], "span_s": round(span, 4),
+                   "offered_edges_per_s": round(E_trace / max(trace_t[-1], 1e-9), 1),
+                   "results": "every request bit-identical to its graph scored alone"},
+        "plain": {"value": E_trace / plain_s, "unit": UNIT, "seconds": round(plain_s, 4),
+                  "p50_ms": round(plat[len(plat) // 2], 3),
+                  "p99_ms": round(plat[min(len(plat) - 1, int(np.ceil(0.99 * len(plat))) - 1)], 3),
+                  "what": "the same requests one at a time: jx_jaccard + copy-out (resident), "
+                          "jx_jaccard_host (uploads); latencies of a one-at-a-time server under the "
+                          "same arrivals from the measured service times"},
+        "served_over_plain": round(value / (E_trace / plain_s), 3),
+        "clocks": clocks,
+        "e2e": {"value": value * world, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": 4 * E_trace,
+                "timing": "served path is end to end: host arrays in, host results out; step = the trace"},
+        "gpu_launches": st["kernels"],
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                     "kernel": "served passes (algorithmic bytes of every request / span)",
+                     "algorithmic_bytes": B},
+    }
+    srv.close()
+    return result
+
+
 # ------------------------------------------------------------------ GPU arm
 
 def run_gpu(args, world, rank, local):
@@ -539,6 +719,28 @@ def run_reference(args, world, rank):
     if rank != 0:
         return None
     threads = os.cpu_count() or 1
+    if args.workload == "served":
+        jx = importlib.import_module("sycl-jaccard_gb300")
+        res, up, st_res, st_up = make_served(threads)
+        _, trace_g = jx.graphgen.poisson_trace(args.requests, args.rate, len(res), len(up), seed=6)
+        pick = [(res if k == "resident" else up)[i] for k, i in trace_g]
+        pst = [(st_res if k == "resident" else st_up)[i] for k, i in trace_g]
+        vals, cb = [], None
+        for i in range(args.warmup + args.steps):
+            cb = cpu_reference_batch(pick, pst, args.cpu_seconds / max(1, args.steps),
+                                     weights=[g[2] for g in pick], what="requests of the trace")
+            if i >= args.warmup:
+                vals.append(cb["value"])
+        value = statistics.median(vals)
+        cb["value"] = value
+        return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "impl": "reference",
+                "config": {"workload": f"served: {args.requests} requests (see the jx arm), serial reference calls",
+                           "algorithm": "vertex_centric", "weighted": True},
+                "cpu_baseline": cb,
+                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if args.workload == "batched":
         graphs, st = make_batch(threads)
         vals, cb = [], None
@@ -583,7 +785,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="jx", choices=["jx", "reference"])
-    ap.add_argument("--workload", default="rmat24w", choices=["rmat24w", "rmat20", "er4096", "batched"])
+    ap.add_argument("--workload", default="rmat24w", choices=["rmat24w", "rmat20", "er4096", "batched", "served"])
+    ap.add_argument("--requests", type=int, default=1000, help="served: requests in the trace")
+    ap.add_argument("--rate", type=float, default=2000.0, help="served: Poisson arrival rate (1/s)")
+    ap.add_argument("--slots", type=int, default=4, help="served: passes in flight")
+    ap.add_argument("--fold-edges", type=int, default=1 << 21, help="served: fold requests up to this size")
+    ap.add_argument("--max-outstanding", type=int, default=256, help="served: result buffers held at once")
     ap.add_argument("--ec", action="store_true", help="edge-centric algorithm")
     ap.add_argument("--unweighted", action="store_true", help="drop the vertex weights")
     ap.add_argument("--weighted", action="store_true",
@@ -601,6 +808,8 @@ def main():
         res = run_reference(args, world, rank)
     elif args.workload == "batched":
         res = run_gpu_batched(args, world, rank, local)
+    elif args.workload == "served":
+        res = run_gpu_served(args, world, rank, local)
     else:
         res = run_gpu(args, world, rank, local)
     if rank == 0 and res is not None:

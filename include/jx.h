@@ -215,6 +215,63 @@ jx_status jx_batch_info(jx_batch b, int64_t *vertices, int64_t *edges, uint64_t 
                         char *plan_desc, size_t len);
 void jx_batch_destroy(jx_batch b);
 
+/* ------------------------------------------------------------------ serving
+ * A request loop on one GPU (this library's addition; the reference has no server).  A
+ * request scores every edge of one graph: a graph kept resident on the device by
+ * jx_server_add_graph (with its row sums when weighted), or a host CSR uploaded with the
+ * request.  Requests are admitted in arrival order while the device-memory budget allows
+ * (resident graphs count against it); small requests that are queued together are folded into
+ * one super-CSR pass (disjoint components, so every request's results are exactly its own);
+ * up to `slots` passes are in flight at once, each on its own stream, so requests that arrive
+ * while others run overlap with them on the device.  Results are written to the request's
+ * host buffer. */
+typedef struct {
+  size_t memory_budget;   /* device bytes for resident graphs + admitted requests */
+  int32_t slots;          /* passes in flight at once (>= 1), one stream and host thread each */
+  int64_t fold_edges;     /* requests of at most this many edges may be folded together */
+  int64_t fold_max_edges; /* edges of one folded pass at most */
+} jx_server_config;
+
+typedef struct {
+  int32_t graph_id;            /* >= 0: a resident graph; -1: upload `graph` */
+  const jx_host_graph *graph;  /* host CSR (weights too when weighted), graph_id == -1 only;
+                                  must stay valid until the request completes */
+  jx_algo algo;
+  int32_t weighted;            /* vertex-centric only: use the graph's vertex weights */
+  float *host_out;             /* e floats, the graph's CSR edge order; written on completion */
+  int64_t arrival_ns;          /* arrival time on jx_server_clock_ns() (0: at submit) */
+} jx_request;
+
+typedef struct {
+  uint64_t completed, failed;
+  uint64_t passes;          /* operator passes run (single or folded) */
+  uint64_t folded_requests; /* requests that shared a pass with others */
+  uint64_t kernels;         /* kernels launched by the passes */
+  int64_t edges;            /* edges scored by completed requests */
+  double p50_ms, p99_ms, mean_ms, max_ms; /* arrival -> results in host memory */
+  double span_s;            /* first arrival -> last completion */
+  size_t peak_reserved;     /* most device bytes admitted at once (resident graphs included) */
+} jx_server_stats;
+
+typedef struct jx_server_s *jx_server;
+
+jx_status jx_server_create(const jx_server_config *cfg, jx_server *out);
+/* Upload a graph to stay resident (row sums computed now when weighted); synchronous. */
+jx_status jx_server_add_graph(jx_server s, const jx_host_graph *g, int32_t weighted, int32_t *graph_id);
+/* Queue a request; returns at once.  JX_ERR_TOO_LARGE (at wait) when it alone exceeds the
+ * budget. */
+jx_status jx_server_submit(jx_server s, const jx_request *r, uint64_t *ticket);
+/* Wait for one request; returns its status, *latency_ms its arrival -> completion time. */
+jx_status jx_server_wait(jx_server s, uint64_t ticket, double *latency_ms);
+/* Wait for every request submitted so far. */
+jx_status jx_server_drain(jx_server s);
+jx_status jx_server_get_stats(jx_server s, jx_server_stats *out);
+void jx_server_reset_stats(jx_server s);
+/* The server's clock (monotonic, nanoseconds) for jx_request.arrival_ns. */
+int64_t jx_server_clock_ns(void);
+/* Drains, then releases every resident graph and the server's threads and streams. */
+void jx_server_destroy(jx_server s);
+
 /* ------------------------------------------------------------------ utilities */
 
 /* Validate a CSR on the device; *flags receives JX_CSR_* bits (0 = valid, sorted, symmetric).

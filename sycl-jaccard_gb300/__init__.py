@@ -29,7 +29,7 @@ from . import csrfile  # noqa: F401  (binary CSR files)
 from . import graphgen  # noqa: F401  (synthetic graphs)
 
 __all__ = ["GraphCSRView", "JxError", "jaccard", "jaccard_host", "jaccard_noalloc", "jaccard_list",
-           "count_above", "remove_reverse_edges", "csrfile", "Batch", "rowsum", "fill", "intersect",
+           "count_above", "remove_reverse_edges", "csrfile", "Batch", "Server", "rowsum", "fill", "intersect",
            "weight", "ec_scan", "ec_unweighted", "csr_check", "lib", "launch_count",
            "launch_count_reset", "graphgen"]
 
@@ -55,6 +55,23 @@ class JxError(RuntimeError):
 class _HostGraph(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int32), ("e", ctypes.c_int32), ("row_ptr", ctypes.c_void_p),
                 ("col_idx", ctypes.c_void_p), ("vertex_w", ctypes.c_void_p)]
+
+
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("memory_budget", ctypes.c_size_t), ("slots", ctypes.c_int32), ("fold_edges", ctypes.c_int64),
+                ("fold_max_edges", ctypes.c_int64)]
+
+
+class _Request(ctypes.Structure):
+    _fields_ = [("graph_id", ctypes.c_int32), ("graph", ctypes.POINTER(_HostGraph)), ("algo", ctypes.c_int),
+                ("weighted", ctypes.c_int32), ("host_out", ctypes.c_void_p), ("arrival_ns", ctypes.c_int64)]
+
+
+class _ServerStats(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64), ("passes", ctypes.c_uint64),
+                ("folded_requests", ctypes.c_uint64), ("kernels", ctypes.c_uint64), ("edges", ctypes.c_int64),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
+                ("max_ms", ctypes.c_double), ("span_s", ctypes.c_double), ("peak_reserved", ctypes.c_size_t)]
 
 
 class _Csr(ctypes.Structure):
@@ -102,6 +119,16 @@ def lib() -> ctypes.CDLL:
             "jx_batch_info": ([_VP, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                ctypes.POINTER(ctypes.c_uint64), ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
             "jx_batch_destroy": ([_VP], None),
+            "jx_server_create": ([ctypes.POINTER(_ServerConfig), ctypes.POINTER(_VP)], ctypes.c_int),
+            "jx_server_add_graph": ([_VP, ctypes.POINTER(_HostGraph), i32, ctypes.POINTER(ctypes.c_int32)],
+                                    ctypes.c_int),
+            "jx_server_submit": ([_VP, ctypes.POINTER(_Request), ctypes.POINTER(ctypes.c_uint64)], ctypes.c_int),
+            "jx_server_wait": ([_VP, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+            "jx_server_drain": ([_VP], ctypes.c_int),
+            "jx_server_get_stats": ([_VP, ctypes.POINTER(_ServerStats)], ctypes.c_int),
+            "jx_server_reset_stats": ([_VP], None),
+            "jx_server_clock_ns": ([], ctypes.c_int64),
+            "jx_server_destroy": ([_VP], None),
             "jx_status_string": ([ctypes.c_int], ctypes.c_char_p),
             "jx_version": ([], ctypes.c_int),
             "jx_last_cuda_error": ([], ctypes.c_int),
@@ -391,6 +418,92 @@ class Batch:
         if self._h:
             lib().jx_batch_destroy(self._h)
             self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Serving loop (``jx_server_*``): admission by a device-memory budget, resident graphs
+    with their row sums, folding of queued small requests into one pass, `slots` passes in
+    flight on their own streams.  Requests score every edge of a graph; results land in the
+    host array given at submit."""
+
+    def __init__(self, memory_budget: int, slots: int = 4, fold_edges: int = 1 << 21,
+                 fold_max_edges: int = 1 << 26):
+        _torch()  # a CUDA device must be present
+        cfg = _ServerConfig(memory_budget, slots, fold_edges, fold_max_edges)
+        self._h = ctypes.c_void_p()
+        _check(lib().jx_server_create(ctypes.byref(cfg), ctypes.byref(self._h)), "jx_server_create")
+        self._keep = {}  # ticket -> host objects that must outlive the request
+        self.edges = {}  # resident graph id -> edge count
+
+    @staticmethod
+    def _host_graph(rp, col, w):
+        rp = np.ascontiguousarray(rp, np.int32)
+        col = np.ascontiguousarray(col, np.int32)
+        w = None if w is None else np.ascontiguousarray(w, np.float32)
+        hg = _HostGraph(len(rp) - 1, len(col), rp.ctypes.data, col.ctypes.data,
+                        None if w is None else w.ctypes.data)
+        return hg, (rp, col, w)
+
+    def add_graph(self, row_ptr, col_idx, weights=None) -> int:
+        hg, _keep = self._host_graph(row_ptr, col_idx, weights)
+        gid = ctypes.c_int32()
+        _check(lib().jx_server_add_graph(self._h, ctypes.byref(hg), int(weights is not None), ctypes.byref(gid)),
+               "jx_server_add_graph")
+        self.edges[gid.value] = len(col_idx)
+        return gid.value
+
+    def submit(self, graph, out: np.ndarray, weighted: bool = False, edge_centric: bool = False,
+               arrival_ns: int = 0) -> int:
+        """graph: a resident id, or (row_ptr, col_idx[, weights]) host arrays to upload.
+        out: float32 host array of the graph's edge count."""
+        keep = [out]
+        if isinstance(graph, (int, np.integer)):
+            req = _Request(int(graph), None, ALGO_EDGE_CENTRIC if edge_centric else ALGO_VERTEX_CENTRIC,
+                           int(weighted), out.ctypes.data, arrival_ns)
+        else:
+            hg, arrays = self._host_graph(graph[0], graph[1], graph[2] if len(graph) > 2 else None)
+            keep += [hg, arrays]
+            req = _Request(-1, ctypes.pointer(hg), ALGO_EDGE_CENTRIC if edge_centric else ALGO_VERTEX_CENTRIC,
+                           int(weighted), out.ctypes.data, arrival_ns)
+        t = ctypes.c_uint64()
+        _check(lib().jx_server_submit(self._h, ctypes.byref(req), ctypes.byref(t)), "jx_server_submit")
+        self._keep[t.value] = keep
+        return t.value
+
+    def wait(self, ticket: int) -> float:
+        """Latency (ms, arrival -> results in host memory) of one request; raises on failure."""
+        lat = ctypes.c_double()
+        st = lib().jx_server_wait(self._h, ticket, ctypes.byref(lat))
+        self._keep.pop(ticket, None)
+        _check(st, "jx_server_wait")
+        return lat.value
+
+    def drain(self):
+        _check(lib().jx_server_drain(self._h), "jx_server_drain")
+
+    def stats(self) -> dict:
+        st = _ServerStats()
+        _check(lib().jx_server_get_stats(self._h, ctypes.byref(st)), "jx_server_get_stats")
+        return {k: getattr(st, k) for k, _ in _ServerStats._fields_}
+
+    def reset_stats(self):
+        lib().jx_server_reset_stats(self._h)
+
+    @staticmethod
+    def clock_ns() -> int:
+        return lib().jx_server_clock_ns()
+
+    def close(self):
+        if self._h:
+            lib().jx_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+            self._keep.clear()
 
     def __del__(self):
         try:

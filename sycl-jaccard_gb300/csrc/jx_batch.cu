@@ -62,6 +62,21 @@ __global__ void shift_cols_kernel(int64_t ne, int32_t ngraphs, const int64_t *__
   }
 }
 
+jx_status shift_to_super(int64_t nv, int64_t ne, int32_t ngraphs, const int64_t *vbase, const int64_t *ebase,
+                         int32_t *row_ptr, int32_t *col, cudaStream_t s) {
+  const int sms = sm_count();
+  jx_status st = JX_OK;
+  if (nv > 0) {
+    shift_rows_kernel<<<sms * 8, 256, 0, s>>>(nv, ngraphs, vbase, ebase, row_ptr);
+    if ((st = check_launch()) != JX_OK) return st;
+  }
+  if (ne > 0) {
+    shift_cols_kernel<<<sms * 8, 256, 0, s>>>(ne, ngraphs, vbase, ebase, col);
+    st = check_launch();
+  }
+  return st;
+}
+
 static void free_batch(jx_batch_s *b) {
   if (!b) return;
   if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -101,6 +116,7 @@ jx_status jx_batch_create(const jx_host_graph *graphs, int32_t ngraphs, jx_algo 
   b->weighted = weighted && algo == JX_ALGO_VERTEX_CENTRIC;
   b->vbase.assign(ngraphs + 1, 0);
   b->ebase.assign(ngraphs + 1, 0);
+  int64_t max_deg = 0; // sizes the class streams (fit_plan)
   for (int32_t g = 0; g < ngraphs; ++g) {
     const jx_host_graph &h = graphs[g];
     if (h.n < 0 || h.e < 0 || (h.n == 0 && h.e > 0) || (h.n > 0 && !h.row_ptr) || (h.e > 0 && !h.col_idx) ||
@@ -110,6 +126,7 @@ jx_status jx_batch_create(const jx_host_graph *graphs, int32_t ngraphs, jx_algo 
     }
     b->vbase[g + 1] = b->vbase[g] + h.n;
     b->ebase[g + 1] = b->ebase[g] + h.e;
+    for (int32_t r = 0; r < h.n; ++r) max_deg = std::max<int64_t>(max_deg, (int64_t)h.row_ptr[r + 1] - h.row_ptr[r]);
   }
   b->nv = b->vbase[ngraphs];
   b->ne = b->ebase[ngraphs];
@@ -152,24 +169,21 @@ jx_status jx_batch_create(const jx_host_graph *graphs, int32_t ngraphs, jx_algo 
   JX_TRY(cudaMemcpyAsync(b->d_ebase, b->ebase.data(), sizeof(int64_t) * (ngraphs + 1), cudaMemcpyHostToDevice,
                          b->stream));
   const int sms = sm_count();
-  if (b->nv > 0) {
-    shift_rows_kernel<<<sms * 8, 256, 0, b->stream>>>(b->nv, ngraphs, b->d_vbase, b->d_ebase, b->row_ptr);
-    if ((st = check_launch()) != JX_OK) { free_batch(b); return st; }
-  }
-  if (b->ne > 0) {
-    shift_cols_kernel<<<sms * 8, 256, 0, b->stream>>>(b->ne, ngraphs, b->d_vbase, b->d_ebase, b->col);
-    if ((st = check_launch()) != JX_OK) { free_batch(b); return st; }
+  if ((st = shift_to_super(b->nv, b->ne, ngraphs, b->d_vbase, b->d_ebase, b->row_ptr, b->col, b->stream)) != JX_OK) {
+    free_batch(b);
+    return st;
   }
   JX_TRY(cudaStreamSynchronize(b->stream)); // host arrays may be released after create
   const jx_csr csr{(int32_t)b->nv, (int32_t)b->ne, b->row_ptr, b->col};
   const float *wp = b->weighted ? b->w : nullptr;
 
   // candidate plans (the default first); the autotuner keeps the fastest on this batch
-  std::vector<Plan> plans{default_plan()};
+  const Plan base = fit_plan(default_plan(), b->ne, max_deg);
+  std::vector<Plan> plans{base};
   if (tune)
     for (int m0 : {4, 8, 16})
       for (int m1 : {2, 3, 4}) {
-        Plan P = default_plan();
+        Plan P = base;
         P.b0_ctas = sms * m0;
         P.b1_ctas = sms * m1;
         if (m0 != 8 || m1 != 3) plans.push_back(P);

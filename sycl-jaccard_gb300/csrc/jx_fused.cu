@@ -857,6 +857,20 @@ Plan default_plan() {
   return Plan{sms, sms / kCluster > 0 ? sms / kCluster : 1, kCap, kHubCap, sms * 3, sms * 8};
 }
 
+// Class-stream capacities no larger than a graph can fill: a class of a task holds at most
+// ceil(d / 8) ids, d the length of the list it walks (<= the maximum degree, <= e), and no row
+// of more than kB2Max tasks means no hub units.  Capacities only size buffers (a class that
+// outgrows its buffer resumes from the adjacency list), so a low hint costs speed, not
+// results.  Capacities stay multiples of 4 (int4 reads of a class).
+Plan fit_plan(Plan P, int64_t e, int64_t max_degree) {
+  const int64_t bound = max_degree >= 0 ? std::min<int64_t>(max_degree, e) : e;
+  const int64_t d = std::min<int64_t>(bound, kB2Max);
+  const int cap = (int)(((d + 7) / 8 + 3) / 4 * 4);
+  P.cap_b2 = std::max(4, std::min(P.cap_b2, cap));
+  if (bound <= kB2Max) P.cap_hub = std::min(P.cap_hub, 4);
+  return P;
+}
+
 struct Layout {
   size_t cnt, rows, unit_off, S, scratch, bitmaps, total;
   int64_t words;
@@ -884,13 +898,15 @@ static Layout layout(int32_t n, int32_t e, bool weighted_vc, const Plan &P) {
 
 template <bool kEC, bool kWeighted>
 static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws, const Plan &P,
-                           cudaStream_t s) {
+                           cudaStream_t s, const float *row_sums) {
   const int32_t n = g.n;
   const Layout L = layout(n, g.e, kWeighted, P);
   int32_t *cnt = reinterpret_cast<int32_t *>(ws + L.cnt);
   int32_t *rows = reinterpret_cast<int32_t *>(ws + L.rows);
   int32_t *unit_off = reinterpret_cast<int32_t *>(ws + L.unit_off);
-  float *S = kWeighted ? reinterpret_cast<float *>(ws + L.S) : nullptr;
+  // row sums: computed into the workspace, or given (kept resident by the caller)
+  float *S_ws = kWeighted ? reinterpret_cast<float *>(ws + L.S) : nullptr;
+  const float *S = kWeighted ? (row_sums ? row_sums : S_ws) : nullptr;
   int32_t *scratch = kWeighted ? reinterpret_cast<int32_t *>(ws + L.scratch) : nullptr;
   uint32_t *bitmaps = reinterpret_cast<uint32_t *>(ws + L.bitmaps);
   const int sms = sm_count();
@@ -909,8 +925,8 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
   hub_units_kernel<<<1, 32, 0, s>>>(g.row_ptr, rows, cnt, unit_off);
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("plan", s);
-  if (kWeighted) {
-    if ((st = jx_rowsum(n, g.e, g.row_ptr, g.col_idx, w, S, (jx_stream_t)s)) != JX_OK) return st;
+  if (kWeighted && !row_sums) {
+    if ((st = jx_rowsum(n, g.e, g.row_ptr, g.col_idx, w, S_ws, (jx_stream_t)s)) != JX_OK) return st;
     prof_mark("rowsum", s);
   }
   fill_bits_kernel<<<sms * 4, 256, 0, s>>>(g.e, reinterpret_cast<uint32_t *>(out), kUnwritten);
@@ -971,10 +987,10 @@ static jx_status check_args(const jx_csr *g, jx_algo algo, const float *out_j, b
 }
 
 static jx_status dispatch(const jx_csr &g, const float *vertex_w, float *out_j, jx_algo algo, char *ws,
-                          const Plan &P, cudaStream_t s) {
-  if (algo == JX_ALGO_EDGE_CENTRIC) return run_fused<true, false>(g, nullptr, out_j, ws, P, s);
-  if (vertex_w) return run_fused<false, true>(g, vertex_w, out_j, ws, P, s);
-  return run_fused<false, false>(g, nullptr, out_j, ws, P, s);
+                          const Plan &P, cudaStream_t s, const float *row_sums = nullptr) {
+  if (algo == JX_ALGO_EDGE_CENTRIC) return run_fused<true, false>(g, nullptr, out_j, ws, P, s, nullptr);
+  if (vertex_w) return run_fused<false, true>(g, vertex_w, out_j, ws, P, s, row_sums);
+  return run_fused<false, false>(g, nullptr, out_j, ws, P, s, nullptr);
 }
 
 size_t plan_workspace(int32_t n, int32_t e, bool weighted_vc, const Plan &P) {
@@ -982,13 +998,14 @@ size_t plan_workspace(int32_t n, int32_t e, bool weighted_vc, const Plan &P) {
 }
 
 jx_status run_plan(const jx_csr &g, const float *vertex_w, float *out, jx_algo algo, void *workspace,
-                   const Plan &P, cudaStream_t s) {
+                   const Plan &P, cudaStream_t s, const float *row_sums) {
   bool run;
   const jx_status st = check_args(&g, algo, out, &run);
   if (!run) return st;
   if (!workspace || (reinterpret_cast<uintptr_t>(workspace) & 255u)) return JX_ERR_INVALID;
   const bool weighted = vertex_w != nullptr && algo == JX_ALGO_VERTEX_CENTRIC;
-  return dispatch(g, weighted ? vertex_w : nullptr, out, algo, static_cast<char *>(workspace), P, s);
+  return dispatch(g, weighted ? vertex_w : nullptr, out, algo, static_cast<char *>(workspace), P, s,
+                  weighted ? row_sums : nullptr);
 }
 
 // ---------------------------------------------------------------- fixed-scratch entry point
@@ -1033,7 +1050,7 @@ extern "C" {
 
 size_t jx_jaccard_workspace_size(const jx_csr *g, int weighted, jx_algo algo) {
   if (!g || g->n < 0) return 0;
-  return layout(g->n, g->e, weighted && algo == JX_ALGO_VERTEX_CENTRIC, default_plan()).total;
+  return layout(g->n, g->e, weighted && algo == JX_ALGO_VERTEX_CENTRIC, fit_plan(default_plan(), g->e, -1)).total;
 }
 
 jx_status jx_jaccard_ws(const jx_csr *g, const float *vertex_w, float *out_j, jx_algo algo,
@@ -1042,7 +1059,7 @@ jx_status jx_jaccard_ws(const jx_csr *g, const float *vertex_w, float *out_j, jx
   const jx_status st = check_args(g, algo, out_j, &run);
   if (!run) return st;
   const bool weighted = vertex_w != nullptr && algo == JX_ALGO_VERTEX_CENTRIC; // EC ignores weights
-  const Plan P = default_plan();
+  const Plan P = fit_plan(default_plan(), g->e, -1);
   if (!workspace || workspace_bytes < layout(g->n, g->e, weighted, P).total ||
       (reinterpret_cast<uintptr_t>(workspace) & 255u))
     return JX_ERR_INVALID;

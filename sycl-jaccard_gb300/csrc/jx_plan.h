@@ -19,10 +19,20 @@ struct Plan {
 };
 
 Plan default_plan();
+// P with its class-stream capacities cut to what a graph of e edges and the given maximum
+// degree (-1: unknown) can use; results do not depend on the capacities.
+Plan fit_plan(Plan P, int64_t e, int64_t max_degree);
 // Workspace bytes of one call under plan P.
 size_t plan_workspace(int32_t n, int32_t e, bool weighted_vc, const Plan &P);
 // The fused operator under plan P (arguments as jx_jaccard_ws; workspace >= plan_workspace).
+// row_sums (weighted vertex-centric only): per-vertex sums of the neighbours' weights computed
+// earlier (jx_rowsum) and kept on the device; the call then skips its row-sum kernel.
 jx_status run_plan(const jx_csr &g, const float *vertex_w, float *out, jx_algo algo, void *workspace,
-                   const Plan &P, cudaStream_t s);
+                   const Plan &P, cudaStream_t s, const float *row_sums = nullptr);
+
+// Turn graph-local row offsets / column ids packed back to back into super-CSR ones: rows of
+// graph g get +ebase[g], columns +vbase[g] (device arrays of ngraphs + 1 bases).
+jx_status shift_to_super(int64_t nv, int64_t ne, int32_t ngraphs, const int64_t *vbase, const int64_t *ebase,
+                         int32_t *row_ptr, int32_t *col, cudaStream_t s);
 
 } // namespace jx

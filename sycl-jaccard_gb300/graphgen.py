@@ -133,3 +133,45 @@ def batch_graphs(count: int = 2000, seed: int = 5, threads: int = 0, vmin: int =
             rp, col = rmat(sc, int(ef[i]), 0.57, 0.19, 0.19, seed=s, threads=threads)
             out.append((rp, col, f"RMAT scale={sc} ef={int(ef[i])}"))
     return out
+
+
+def served_pools(seed: int = 6, resident: int = 64, uploads: int = 32, threads: int = 0):
+    """The served workload's graphs.  Resident pool: `resident` R-MAT graphs, scale uniform in
+    [14, 20], edge factor 16, (a, b, c) = (.57, .19, .19).  Upload pool: `uploads` graphs with
+    vertex counts log-uniform in [1e3, 1e6], half Erdos-Renyi (avg degree uniform in [4, 64]),
+    half R-MAT (scale round(log2 n), edge factor 16).  Every graph carries per-vertex float32
+    weights uniform in (0, 1].  Returns two lists of (row_ptr, col_idx, weights, description)."""
+    rng = np.random.default_rng(seed)
+    res = []
+    for i, sc in enumerate(rng.integers(14, 21, resident)):
+        s = seed * 1000003 + i
+        rp, col = rmat(int(sc), 16, 0.57, 0.19, 0.19, seed=s, threads=threads)
+        res.append((rp, col, uniform_weights(len(rp) - 1, seed=s + 500000, threads=threads),
+                    f"RMAT scale={int(sc)} ef=16"))
+    up = []
+    nv = np.exp(rng.uniform(np.log(1e3), np.log(1e6), uploads)).round().astype(np.int64)
+    deg = rng.uniform(4.0, 64.0, uploads)
+    for i in range(uploads):
+        s = seed * 1000003 + 700000 + i
+        n = int(nv[i])
+        if i % 2 == 0:
+            rp, col = er_gnm(n, int(round(n * deg[i] / 2)), seed=s, threads=threads)
+            d = f"ER n={n} deg={deg[i]:.1f}"
+        else:
+            sc = int(np.round(np.log2(n)))
+            rp, col = rmat(sc, 16, 0.57, 0.19, 0.19, seed=s, threads=threads)
+            d = f"RMAT scale={sc} ef=16"
+        up.append((rp, col, uniform_weights(len(rp) - 1, seed=s + 500000, threads=threads), d))
+    return res, up
+
+
+def poisson_trace(count: int, rate: float, resident: int, uploads: int, seed: int = 6,
+                  resident_share: float = 0.7):
+    """Arrival times (s, from 0) of a Poisson stream of `count` requests at `rate` per second,
+    and their targets: ("resident", k) with probability resident_share, else ("upload", k)."""
+    rng = np.random.default_rng(seed + 1)
+    t = np.cumsum(rng.exponential(1.0 / rate, count))
+    is_res = rng.random(count) < resident_share
+    k_res = rng.integers(0, resident, count)
+    k_up = rng.integers(0, uploads, count)
+    return t - t[0], [("resident", int(a)) if r else ("upload", int(b)) for r, a, b in zip(is_res, k_res, k_up)]
