@@ -204,7 +204,9 @@ typedef struct jx_batch_s *jx_batch;
 /* Copies the graphs to the device (synchronous; the host arrays may be freed afterwards). */
 jx_status jx_batch_create(const jx_host_graph *graphs, int32_t ngraphs, jx_algo algo, int weighted,
                           int tune, jx_batch *out);
-/* One pass over every graph of the batch (asynchronous on `stream`). */
+/* One pass over every graph of the batch (asynchronous on `stream`).  Passes of one batch
+ * share its workspace and outputs: do not let two of them overlap (issue them on one stream,
+ * or synchronise between streams). */
 jx_status jx_batch_run(jx_batch b, jx_stream_t stream);
 /* Device slice of graph g's results (valid until destroy). */
 jx_status jx_batch_result(jx_batch b, int32_t g, const float **device_out, int64_t *count);

@@ -234,6 +234,9 @@ jx_status jx_batch_create(const jx_host_graph *graphs, int32_t ngraphs, jx_algo 
     jx_launch_count_reset(); // the capture itself launched nothing
     count_launches(before);
     JX_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    // the warm-up pass ran on the batch's own stream: it must end before a replay on the
+    // caller's stream touches the same workspace and outputs
+    JX_TRY(cudaStreamSynchronize(b->stream));
   }
   b->plan_desc = describe(b->plan);
 #undef JX_TRY

@@ -87,7 +87,7 @@ def _mixed_graphs(jx, count, seed):
 
 
 @pytest.mark.parametrize("mode", ["ec", "vc", "vcw"])
-def test_batch_equals_per_graph(jx, mode):
+def test_batch_equals_per_graph(jx, O, mode):
     import torch
     gs = _mixed_graphs(jx, 24, 3)
     b = jx.Batch(gs, edge_centric=(mode == "ec"), weighted=(mode == "vcw"), tune=(mode == "vc"))
@@ -102,5 +102,15 @@ def test_batch_equals_per_graph(jx, mode):
             g = jx.GraphCSRView.from_numpy(rp, col)
             want = jx.jaccard(g, torch.from_numpy(w).cuda() if mode == "vcw" else None,
                               edge_centric=(mode == "ec")).cpu().numpy()
-            assert np.array_equal(bits(b.download(i)), bits(want)), (rep, i)
+            got = b.download(i)
+            bad = np.nonzero(bits(got) != bits(want))[0]
+            if len(bad):
+                ora = O.jaccard(rp, col, w if mode == "vcw" else None, edge_centric=(mode == "ec"))
+                d = np.diff(rp)
+                src = np.repeat(np.arange(len(rp) - 1), d)
+                info = [(int(k), int(src[k]), int(col[k]), int(d[src[k]]), int(d[col[k]]), float(got[k]),
+                         float(want[k]), float(ora[k])) for k in bad[:6]]
+                raise AssertionError(f"rep {rep} graph {i}: {len(bad)} differ; batch!=oracle "
+                                     f"{int((bits(got) != bits(ora)).sum())}, plain!=oracle "
+                                     f"{int((bits(want) != bits(ora)).sum())}; (k,u,v,du,dv,batch,plain,oracle) {info}")
     b.close()
