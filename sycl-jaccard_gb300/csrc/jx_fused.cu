@@ -204,10 +204,27 @@ template <bool kGlobal> struct Streams {
     return acc;
   }
 };
-// All classes at once when none overflowed: lane i takes the i-th matched id in class-major
-// order (class c starts at the prefix sum of the counts of classes < c), gathers its weight,
-// and the warp folds 32 values per round in order.  counts: lane c (c < 8) holds class c's
-// count, other lanes 0.  acc uniform.
+// All classes at once when none overflowed.  The matched ids are taken in class-major order
+// (class c starts at the prefix sum of the counts of classes < c) 128 per round: lane L holds
+// entries 4L .. 4L+3 of the round, gathers their weights, and the warp folds the 128 values in
+// order through shuffles with constant lane indices.  The ids of the next round are loaded
+// before the current round is folded, so a round waits on one gather, not on an id load and
+// a gather.  counts: lane c (c < 8) holds class c's count, other lanes 0.  acc uniform.
+template <class S>
+__device__ __forceinline__ int32_t class_entry(const S &cls, const int32_t (&start)[8], int32_t i,
+                                               int32_t total) {
+  if (i >= total) return -1;
+  int c = 0;
+  int32_t sc = 0;
+#pragma unroll
+  for (int q = 1; q < 8; ++q)
+    if (i >= start[q]) {
+      c = q;
+      sc = start[q];
+    }
+  return cls.get(c, i - sc);
+}
+
 template <class S>
 __device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, const float *__restrict__ w,
                                           float acc) {
@@ -222,28 +239,27 @@ __device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, const 
   int32_t start[8];
 #pragma unroll
   for (int c = 0; c < 8; ++c) start[c] = __shfl_sync(kFull, incl - my_count, c);
-  for (int32_t t = 0; t < total; t += 32) {
-    const int32_t i = t + lane;
-    float v = 0.0f;
-    if (i < total) {
-      int c = 0;
-      int32_t sc = 0;
+  int32_t id[4];
 #pragma unroll
-      for (int q = 1; q < 8; ++q)
-        if (i >= start[q]) {
-          c = q;
-          sc = start[q];
-        }
-      v = __ldg(w + cls.get(c, i - sc));
+  for (int m = 0; m < 4; ++m) id[m] = class_entry(cls, start, 4 * lane + m, total);
+  for (int32_t t = 0; t < total; t += 128) {
+    float v[4];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) v[m] = id[m] >= 0 ? __ldg(w + id[m]) : 0.0f;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) id[m] = class_entry(cls, start, t + 128 + 4 * lane + m, total);
+    const int32_t k = total - t < 128 ? total - t : 128;
+#pragma unroll
+    for (int L = 0; L < 32; ++L) {
+      if (4 * L < k) {
+        const float a = __shfl_sync(kFull, v[0], L), b = __shfl_sync(kFull, v[1], L);
+        const float c = __shfl_sync(kFull, v[2], L), d = __shfl_sync(kFull, v[3], L);
+        acc = a + acc;
+        if (4 * L + 1 < k) acc = b + acc;
+        if (4 * L + 2 < k) acc = c + acc;
+        if (4 * L + 3 < k) acc = d + acc;
+      }
     }
-    const int32_t k = total - t < 32 ? total - t : 32;
-    int b = 0;
-    for (; b + 4 <= k; b += 4) {
-      const float v0 = __shfl_sync(kFull, v, b), v1 = __shfl_sync(kFull, v, b + 1);
-      const float v2 = __shfl_sync(kFull, v, b + 2), v3 = __shfl_sync(kFull, v, b + 3);
-      acc = v0 + acc; acc = v1 + acc; acc = v2 + acc; acc = v3 + acc;
-    }
-    for (; b < k; ++b) acc = __shfl_sync(kFull, v, b) + acc;
   }
   return acc;
 }
@@ -574,6 +590,14 @@ __device__ __forceinline__ void run_batch(const Probe &probe, const Streams &cls
   }
 }
 
+// Tasks a warp takes at once from a row (or hub unit) shared by `warps` warps, `rem` tasks
+// left: 32 while plenty remain, then smaller batches so that the warps finish the row close
+// together (they meet at a barrier before the next row).
+__device__ __forceinline__ int32_t guided_batch(int32_t rem, int warps) {
+  const int32_t g = rem / (2 * warps);
+  return g >= 32 ? 32 : (g < 2 ? 2 : g);
+}
+
 // Cuckoo table size for d keys: 2.5 slots per key (even), at most `cap` slots.
 __device__ __forceinline__ uint32_t cuckoo_slots(int32_t d, uint32_t cap) {
   uint32_t s = ((5u * (uint32_t)d + 3u) / 2u + 1u) & ~1u;
@@ -637,11 +661,15 @@ __device__ __forceinline__ void b2_tasks(const Probe &probe, const ClassStreams 
   const int lane = threadIdx.x & 31;
   const float Su = kWeighted ? __ldg(S + u) : 0.0f;
   for (;;) {
-    int32_t k0 = 0;
-    if (lane == 0) k0 = atomicAdd(s_task, 32);
+    int32_t k0 = 0, g = 0;
+    if (lane == 0) {
+      g = guided_batch(du - *(volatile int32_t *)s_task, kB2Threads / 32);
+      k0 = atomicAdd(s_task, g);
+    }
     k0 = __shfl_sync(kFull, k0, 0);
+    g = __shfl_sync(kFull, g, 0);
     if (k0 >= du) break;
-    run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, du, out);
+    run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, min(du, k0 + g), out);
   }
 }
 
@@ -742,11 +770,15 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
     const BitmapProbe probe{bm};
     const float Su = kWeighted ? __ldg(S + u) : 0.0f;
     for (;;) {
-      int32_t k0 = 0;
-      if (lane == 0) k0 = k_begin + atomicAdd(task_p, 32);
+      int32_t k0 = 0, g = 0;
+      if (lane == 0) {
+        g = guided_batch(k_end - k_begin - *(volatile int32_t *)task_p, kCluster * (kHubThreads / 32));
+        k0 = k_begin + atomicAdd(task_p, g);
+      }
       k0 = __shfl_sync(kFull, k0, 0);
+      g = __shfl_sync(kFull, g, 0);
       if (k0 >= k_end) break;
-      run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, k_end, out);
+      run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, min(k_end, k0 + g), out);
     }
     cluster.sync();
     for (int32_t k = rank * blockDim.x + threadIdx.x; k < du; k += kCluster * blockDim.x)

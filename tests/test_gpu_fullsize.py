@@ -61,3 +61,20 @@ def test_rmat20_weighted_samples(jx, O, rmat20):
                                  w.ctypes.data_as(O._F32), r0, r1, S.ctypes.data_as(O._F32),
                                  want.ctypes.data_as(O._F32), 0)
         assert np.array_equal(bits(J[rp[r0]:rp[r1]]), bits(want)), (r0, r1)
+
+
+def test_weighted_error_vs_fp64(jx, O):
+    """Weighted VC on RMAT-16: bit-identical to the reference's order (so <= 1e-6 relative
+    from the reference), and the error of that order against an FP64 evaluation of the same
+    formula stays below 1e-5 relative (printed)."""
+    import torch
+    rp, col = jx.graphgen.rmat(16, 16, 0.57, 0.19, 0.19, seed=21)
+    w = jx.graphgen.uniform_weights(len(rp) - 1, seed=22)
+    g = jx.GraphCSRView.from_numpy(rp, col)
+    J = jx.jaccard(g, torch.from_numpy(w).cuda()).cpu().numpy()
+    assert np.array_equal(bits(J), bits(O.jaccard(rp, col, w)))
+    J64 = O.jaccard_f64(rp, col, w)
+    err = np.abs(J.astype(np.float64) - J64)
+    rel = err / np.maximum(np.abs(J64), 1e-300)
+    print(f"weighted RMAT-16 vs FP64: max abs {err.max():.3e}, max rel {rel[J64 > 0].max():.3e}")
+    assert rel[J64 > 0].max() < 1e-5
