@@ -337,8 +337,12 @@ __device__ __forceinline__ void task_chunk(const Probe &probe, const int32_t *__
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     if (kTail) {
-      const int32_t key = x[j] != kEmpty ? x[j] : 0;
-      f[j] = (x[j] != kEmpty) & probe(key);
+      // rows of the tail past the end of the list (warp-uniform test) probe nothing
+      f[j] = false;
+      if (base + 32 * j < dv) {
+        const int32_t key = x[j] != kEmpty ? x[j] : 0;
+        f[j] = (x[j] != kEmpty) & probe(key);
+      }
     } else {
       f[j] = probe(x[j]);
     }
