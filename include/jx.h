@@ -183,6 +183,24 @@ jx_status jx_count_above(int64_t e, const float *values, float thresh, unsigned 
 jx_status jx_remove_reverse_edges(const jx_csr *g, const float *values, int32_t *src, int32_t *dst,
                                   float *out_values, int64_t *count, jx_stream_t stream);
 
+/* Graph preparation of the reference's driver on the device (main.cpp:99-118: reverse edges
+ * added to the MTX set, then mtxSetToCSR, readMtxToCSR.cpp:117-208): from an edge list to a
+ * CSR with every row sorted ascending, no repeated neighbour and, unless kept, no self loop.
+ *   src, dst   device int32[m], zero-based vertex ids in [0, n) (else JX_ERR_INVALID);
+ *   flags      JX_BUILD_SYMMETRIZE adds (v, u) for every (u, v) (the reference's
+ *              invertDirection for undirected input); JX_BUILD_KEEP_SELF_LOOPS keeps (u, u);
+ *   row_ptr    device int32[n + 1] out; col device int32[cap] out (cap >= m, or 2m when
+ *              symmetrising, always suffices); *e_out (host) the number of stored edges.
+ * Unlike the reference, every vertex in [0, n) keeps its row (the reference's rows start at the
+ * first source and end at the last, readMtxToCSR.cpp:158-179), and edge values are not
+ * carried (the operators use per-vertex weights).  JX_ERR_TOO_LARGE when the result exceeds
+ * cap or 2^31 - 1 edges.  Synchronous on `stream` (it reads back the edge count);
+ * temporaries (about 40 bytes per input edge) from the stream-ordered allocator. */
+#define JX_BUILD_SYMMETRIZE 0x1u
+#define JX_BUILD_KEEP_SELF_LOOPS 0x2u
+jx_status jx_csr_build(int32_t n, int64_t m, const int32_t *src, const int32_t *dst, uint32_t flags,
+                       int32_t *row_ptr, int32_t *col, int64_t cap, int64_t *e_out, jx_stream_t stream);
+
 /* ------------------------------------------------------------------ batched mode
  * Many graphs packed into one offset-indexed super-CSR on the device (graph g's vertex ids
  * shifted by the vertices before it, its edges by the edges before it; at most 2^31 - 1

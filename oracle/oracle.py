@@ -241,3 +241,45 @@ def ref_remove_reverse(row_ptr, col, values):
     k = ref_lib().jxref_remove_reverse(len(row_ptr) - 1, e, _p(row_ptr, _I32), _p(col, _I32),
                                        _p(values, _F32), _p(src, _I32), _p(dst, _I32), _p(val, _F32), e)
     return src[:k], dst[:k], val[:k]
+
+
+def ref_csr_from_edges(src, dst, symmetrize=True, keep_self=False):
+    """The reference's own graph preparation (main.cpp:99-118: MTX set, invertDirection,
+    mtxSetToCSR) on a zero-based edge list.  Returns (row_ptr, col) of the CSR it builds,
+    whose rows run from the first source vertex to the last (readMtxToCSR.cpp:158-179)."""
+    src = np.ascontiguousarray(src, np.int32)
+    dst = np.ascontiguousarray(dst, np.int32)
+    m = len(src)
+    cap = 2 * m + 1
+    nv_cap = int(max(src.max(), dst.max())) + 2 if m else 1
+    offsets = np.empty(nv_cap + 1, np.int32)
+    indices = np.empty(cap, np.int32)
+    nv = ctypes.c_int32()
+    L = ref_lib()
+    L.jxref_csr_from_edges.restype = ctypes.c_int64
+    L.jxref_csr_from_edges.argtypes = [ctypes.c_int64, _I32, _I32, ctypes.c_int, ctypes.c_int, _I32,
+                                       ctypes.c_int64, _I32, ctypes.c_int64, ctypes.POINTER(ctypes.c_int32)]
+    e = L.jxref_csr_from_edges(m, _p(src, _I32), _p(dst, _I32), int(symmetrize), int(keep_self),
+                               _p(offsets, _I32), nv_cap + 1, _p(indices, _I32), cap, ctypes.byref(nv))
+    if e < 0:
+        raise RuntimeError(f"reference CSR build failed ({e})")
+    return offsets[: nv.value + 1].copy(), indices[:e].copy()
+
+
+def csr_build(n, src, dst, symmetrize=True, keep_self=False):
+    """Restatement of the graph preparation with every vertex of [0, n) keeping its row: the
+    set of (u, v) pairs (and (v, u) when symmetrising, main.cpp:99-111, readMtxToCSR.cpp:117-132)
+    in ascending order, self loops dropped unless kept (readMtxToCSR.cpp:174), as a CSR."""
+    src = np.asarray(src, np.int64)
+    dst = np.asarray(dst, np.int64)
+    if symmetrize:
+        src, dst = np.concatenate([src, dst]), np.concatenate([dst, src])
+    if not keep_self:
+        keep = src != dst
+        src, dst = src[keep], dst[keep]
+    keys = np.unique(src * n + dst)
+    rows = keys // n
+    col = (keys % n).astype(np.int32)
+    row_ptr = np.zeros(n + 1, np.int64)
+    np.add.at(row_ptr, rows + 1, 1)
+    return np.cumsum(row_ptr).astype(np.int32), col

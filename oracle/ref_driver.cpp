@@ -20,6 +20,8 @@
  *   jxref_csr_write      CSRToFile<int32_t,int32_t,float>        (readMtxToCSR.cpp:285-337)
  *   jxref_csr_read       FileToCSR                                 (readMtxToCSR.cpp:388-395)
  *   jxref_remove_reverse CSRToMtx + removeReverseEdges             (readMtxToCSR.cpp:134-147, 211-248)
+ *   jxref_csr_from_edges MTX set + invertDirection + mtxSetToCSR    (main.cpp:99-118,
+ *                        readMtxToCSR.cpp:117-132, 153-208)
  * The edge-centric driver prints a line to std::cout (jaccard.cpp:819); it is discarded.
  */
 #include "jaccard.cpp"
@@ -231,6 +233,42 @@ int64_t jxref_remove_reverse(int32_t n, int32_t e, const int32_t *offsets, const
   }
   delete m;
   return k;
+}
+
+/* The driver's graph preparation (main.cpp:99-118) on a zero-based edge list: the edges as
+ * an MTX set (one-based ids, weight 1), the set's invertDirection inserted when symmetrising,
+ * then mtxSetToCSR (self loops dropped unless keep_self).  Writes the CSR's offsets and
+ * indices; *nv receives its number of rows (the reference's rows run from the first source to
+ * the last).  Returns the number of edges, or -1 when a capacity is too small, -2 when the
+ * list is empty. */
+int64_t jxref_csr_from_edges(int64_t m, const int32_t *src, const int32_t *dst, int symmetrize, int keep_self,
+                             int32_t *offsets, int64_t offsets_cap, int32_t *indices, int64_t cap,
+                             int32_t *nv) {
+  if (m <= 0) return -2;
+  std::set<std::tuple<int32_t, int32_t, float>> mtx;
+  for (int64_t i = 0; i < m; ++i) mtx.insert(std::tuple<int32_t, int32_t, float>(src[i] + 1, dst[i] + 1, 1.0f));
+  if (symmetrize) {
+    std::set<std::tuple<int32_t, int32_t, float>> *rev = invertDirection(mtx);
+    mtx.insert(rev->begin(), rev->end());
+    delete rev;
+  }
+  GraphCSRView<int32_t, int32_t, float> *g = mtxSetToCSR(mtx, !keep_self, false);
+  const int64_t n = g->number_of_vertices, e = g->number_of_edges;
+  if (n + 1 > offsets_cap || e > cap) {
+    delete g;
+    return -1;
+  }
+  {
+    auto o = g->offsets.get_access<cl::sycl::access::mode::read>();
+    std::memcpy(offsets, &o[0], sizeof(int32_t) * (size_t)(n + 1));
+    if (e > 0) {
+      auto ix = g->indices.get_access<cl::sycl::access::mode::read>();
+      std::memcpy(indices, &ix[0], sizeof(int32_t) * (size_t)e);
+    }
+  }
+  *nv = (int32_t)n;
+  delete g;
+  return e;
 }
 
 } /* extern "C" */

@@ -29,7 +29,7 @@ from . import csrfile  # noqa: F401  (binary CSR files)
 from . import graphgen  # noqa: F401  (synthetic graphs)
 
 __all__ = ["GraphCSRView", "JxError", "jaccard", "jaccard_host", "jaccard_noalloc", "jaccard_list",
-           "count_above", "remove_reverse_edges", "csrfile", "Batch", "Server", "rowsum", "fill", "intersect",
+           "count_above", "remove_reverse_edges", "csrfile", "Batch", "Server", "csr_build", "rowsum", "fill", "intersect",
            "weight", "ec_scan", "ec_unweighted", "csr_check", "lib", "launch_count",
            "launch_count_reset", "graphgen"]
 
@@ -110,6 +110,8 @@ def lib() -> ctypes.CDLL:
             "jx_csr_check": ([ctypes.POINTER(_Csr), u32p, _VP], ctypes.c_int),
             "jx_jaccard_list": ([ctypes.POINTER(_Csr), _VP, i64, _VP, _VP, _VP, _VP], ctypes.c_int),
             "jx_count_above": ([i64, _VP, f32, _VP, _VP], ctypes.c_int),
+            "jx_csr_build": ([i32, i64, _VP, _VP, ctypes.c_uint32, _VP, _VP, i64, ctypes.POINTER(ctypes.c_int64),
+                              _VP], ctypes.c_int),
             "jx_remove_reverse_edges": ([ctypes.POINTER(_Csr), _VP, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
             "jx_batch_create": ([ctypes.POINTER(_HostGraph), i32, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                  ctypes.POINTER(_VP)], ctypes.c_int),
@@ -349,6 +351,31 @@ def count_above(values, thresh: float = 1e-5, stream=None) -> int:
     _check(lib().jx_count_above(values.numel(), _ptr(values, torch.float32, values.numel(), "values"),
                                 float(thresh), ctypes.c_void_p(c.data_ptr()), _stream(stream)), "jx_count_above")
     return int(c.item())
+
+
+BUILD_SYMMETRIZE = 0x1
+BUILD_KEEP_SELF_LOOPS = 0x2
+
+
+def csr_build(n: int, src, dst, symmetrize: bool = True, keep_self: bool = False, stream=None) -> GraphCSRView:
+    """The driver's graph preparation on the device (main.cpp:99-118, readMtxToCSR.cpp:117-208):
+    int32 device edge lists `src`, `dst` (zero-based) -> a CSR with sorted, duplicate-free rows,
+    reverse edges added when `symmetrize`, self loops dropped unless `keep_self`."""
+    torch = _torch()
+    m = src.numel()
+    if dst.numel() != m:
+        raise ValueError("src and dst differ in length")
+    dev = src.device if m else torch.device("cuda")
+    cap = max(1, 2 * m if symmetrize else m)
+    row_ptr = torch.empty(n + 1, dtype=torch.int32, device=dev)
+    col = torch.empty(cap, dtype=torch.int32, device=dev)
+    e = ctypes.c_int64()
+    flags = (BUILD_SYMMETRIZE if symmetrize else 0) | (BUILD_KEEP_SELF_LOOPS if keep_self else 0)
+    _check(lib().jx_csr_build(n, m, _ptr(src, torch.int32, m, "src") if m else None,
+                              _ptr(dst, torch.int32, m, "dst") if m else None, flags,
+                              ctypes.c_void_p(row_ptr.data_ptr()), ctypes.c_void_p(col.data_ptr()), cap,
+                              ctypes.byref(e), _stream(stream)), "jx_csr_build")
+    return GraphCSRView(row_ptr, col[: e.value].clone(), None, n, e.value)
 
 
 def remove_reverse_edges(graph: GraphCSRView, values, stream=None):
