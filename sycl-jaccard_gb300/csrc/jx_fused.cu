@@ -46,6 +46,7 @@ constexpr int32_t kB0Max = 32, kB1Max = 512, kB2Max = 24576;
 constexpr int kB0Slots = 64;
 constexpr int kB1Slots = 1280;   // cuckoo, 2.5 slots per element at d = 512
 constexpr int kB2Slots = 58000;  // cuckoo, <= 227 KB; load factor <= 0.424 at d = kB2Max
+constexpr int kB2FoldWords = (1024 / 32) * 128; // fold buffers of the 32 warps of a B2 CTA
 constexpr int kCuckooMaxEvict = 64;
 constexpr int kCuckooSeeds = 4;
 constexpr int kB2Threads = 1024;
@@ -163,6 +164,7 @@ struct SearchProbe {
 template <bool kGlobal> struct Streams {
   int32_t *base;
   int cap;
+  float *fbuf = nullptr; // shared memory, 128 floats of this warp for the fold, or none
   __device__ __forceinline__ void put(int c, int pos, int32_t x) const {
     if (kGlobal) __stcg(base + c * cap + pos, x); else base[c * cap + pos] = x;
   }
@@ -204,25 +206,28 @@ template <bool kGlobal> struct Streams {
     return acc;
   }
 };
+template <class S> struct kIsGlobal;
+template <bool G> struct kIsGlobal<Streams<G>> { static constexpr bool value = G; };
+
 // All classes at once when none overflowed.  The matched ids are taken in class-major order
 // (class c starts at the prefix sum of the counts of classes < c) 128 per round: lane L holds
-// entries 4L .. 4L+3 of the round, gathers their weights, and the warp folds the 128 values in
-// order through shuffles with constant lane indices.  The ids of the next round are loaded
-// before the current round is folded, so a round waits on one gather, not on an id load and
-// a gather.  counts: lane c (c < 8) holds class c's count, other lanes 0.  acc uniform.
+// entries 4L .. 4L+3 of the round and gathers their weights; the ids of the next round are
+// loaded before the current round is folded, so a round waits on one gather, not on an id
+// load and a gather.  The warp then adds the 128 values in order: from a shared-memory copy
+// (one broadcast 16-byte read per 4 values) when the warp has a fold buffer, else through
+// shuffles with constant lane indices; full rounds run without per-value tests.
+// counts: lane c (c < 8) holds class c's count, other lanes 0.  acc uniform.
+//
+// Entry i of class c sits at c * cap + (i - start[c]); with d[q] = cap - count[q - 1] that is
+// i + the sum of d[q] over the classes q >= 1 that start at or before i.
 template <class S>
-__device__ __forceinline__ int32_t class_entry(const S &cls, const int32_t (&start)[8], int32_t i,
-                                               int32_t total) {
+__device__ __forceinline__ int32_t class_entry(const S &cls, const int32_t (&start)[8], const int32_t (&d)[8],
+                                               int32_t i, int32_t total) {
   if (i >= total) return -1;
-  int c = 0;
-  int32_t sc = 0;
+  int32_t off = i;
 #pragma unroll
-  for (int q = 1; q < 8; ++q)
-    if (i >= start[q]) {
-      c = q;
-      sc = start[q];
-    }
-  return cls.get(c, i - sc);
+  for (int q = 1; q < 8; ++q) off += i >= start[q] ? d[q] : 0;
+  return kIsGlobal<S>::value ? __ldcg(cls.base + off) : cls.base[off];
 }
 
 template <class S>
@@ -236,31 +241,70 @@ __device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, const 
     if (lane >= o) incl += y;
   }
   const int32_t total = __shfl_sync(kFull, incl, 7);
-  int32_t start[8];
+  int32_t start[8], d[8];
 #pragma unroll
   for (int c = 0; c < 8; ++c) start[c] = __shfl_sync(kFull, incl - my_count, c);
+  d[0] = 0;
+#pragma unroll
+  for (int q = 1; q < 8; ++q) d[q] = cls.cap - (start[q] - start[q - 1]);
   int32_t id[4];
 #pragma unroll
-  for (int m = 0; m < 4; ++m) id[m] = class_entry(cls, start, 4 * lane + m, total);
+  for (int m = 0; m < 4; ++m) id[m] = class_entry(cls, start, d, 4 * lane + m, total);
+  float4 *const buf = reinterpret_cast<float4 *>(cls.fbuf);
   for (int32_t t = 0; t < total; t += 128) {
     float v[4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) v[m] = id[m] >= 0 ? __ldg(w + id[m]) : 0.0f;
 #pragma unroll
-    for (int m = 0; m < 4; ++m) id[m] = class_entry(cls, start, t + 128 + 4 * lane + m, total);
+    for (int m = 0; m < 4; ++m) id[m] = class_entry(cls, start, d, t + 128 + 4 * lane + m, total);
     const int32_t k = total - t < 128 ? total - t : 128;
+    if (buf) {
+      __syncwarp(); // the previous round's reads are done
+      buf[lane] = make_float4(v[0], v[1], v[2], v[3]);
+      __syncwarp();
+      if (k == 128) {
 #pragma unroll
-    for (int L = 0; L < 32; ++L) {
-      if (4 * L < k) {
+        for (int L = 0; L < 32; ++L) {
+          const float4 q = buf[L];
+          acc = q.x + acc;
+          acc = q.y + acc;
+          acc = q.z + acc;
+          acc = q.w + acc;
+        }
+      } else {
+        for (int L = 0; 4 * L < k; ++L) {
+          const float4 q = buf[L];
+          acc = q.x + acc;
+          if (4 * L + 1 < k) acc = q.y + acc;
+          if (4 * L + 2 < k) acc = q.z + acc;
+          if (4 * L + 3 < k) acc = q.w + acc;
+        }
+      }
+    } else if (k == 128) {
+#pragma unroll
+      for (int L = 0; L < 32; ++L) {
         const float a = __shfl_sync(kFull, v[0], L), b = __shfl_sync(kFull, v[1], L);
-        const float c = __shfl_sync(kFull, v[2], L), d = __shfl_sync(kFull, v[3], L);
+        const float c = __shfl_sync(kFull, v[2], L), e = __shfl_sync(kFull, v[3], L);
         acc = a + acc;
-        if (4 * L + 1 < k) acc = b + acc;
-        if (4 * L + 2 < k) acc = c + acc;
-        if (4 * L + 3 < k) acc = d + acc;
+        acc = b + acc;
+        acc = c + acc;
+        acc = e + acc;
+      }
+    } else {
+#pragma unroll
+      for (int L = 0; L < 32; ++L) {
+        if (4 * L < k) {
+          const float a = __shfl_sync(kFull, v[0], L), b = __shfl_sync(kFull, v[1], L);
+          const float c = __shfl_sync(kFull, v[2], L), e = __shfl_sync(kFull, v[3], L);
+          acc = a + acc;
+          if (4 * L + 1 < k) acc = b + acc;
+          if (4 * L + 2 < k) acc = c + acc;
+          if (4 * L + 3 < k) acc = e + acc;
+        }
       }
     }
   }
+  if (buf) __syncwarp();
   return acc;
 }
 
@@ -610,7 +654,8 @@ __device__ __forceinline__ uint32_t cuckoo_slots(int32_t d, uint32_t cap) {
 }
 
 // ---------------------------------------------------------------- B1: warp per row
-// Dynamic shared memory per warp: kB1Slots table slots, then (weighted) 8 * kB1Cap floats.
+// Dynamic shared memory per warp: kB1Slots table slots, then (weighted) 8 * kB1Cap class-stream
+// ids.  (Folds here are short -- at most 512 matches -- and use shuffles, not a fold buffer.)
 template <bool kEC, bool kWeighted>
 __global__ void __launch_bounds__(kRowThreads) b1_kernel(
     const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
@@ -712,14 +757,19 @@ __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
       __syncthreads();
       if (!failed) break;
     }
+    // the table uses `slots` words; the last 32 x 128 words of the area, when free, hold the
+    // warps' fold buffers
+    ClassStreams rcls = cls;
+    if (kWeighted && slots + kB2FoldWords <= (uint32_t)kB2Slots)
+      rcls.fbuf = reinterpret_cast<float *>(table + kB2Slots - kB2FoldWords) + wid * 128;
     if (seed < kCuckooSeeds) {
-      b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), cls, &s_task, row_ptr, col, w, S, u, us, du, out);
+      b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), rcls, &s_task, row_ptr, col, w, S, u, us, du, out);
     } else { // eviction cycles with every multiplier: linear probing (load <= 0.43)
       for (uint32_t k = threadIdx.x; k < slots; k += blockDim.x) table[k] = kEmpty;
       __syncthreads();
       for (int32_t k = threadIdx.x; k < du; k += blockDim.x) hset_insert(table, slots, __ldg(col + us + k));
       __syncthreads();
-      b2_tasks<kEC, kWeighted>(HashProbe{table, slots}, cls, &s_task, row_ptr, col, w, S, u, us, du, out);
+      b2_tasks<kEC, kWeighted>(HashProbe{table, slots}, rcls, &s_task, row_ptr, col, w, S, u, us, du, out);
     }
     __syncthreads();
   }
@@ -738,11 +788,13 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
     float *__restrict__ out, int32_t *__restrict__ scratch, int cap) {
   cg::cluster_group cluster = cg::this_cluster();
   __shared__ int32_t s_unit, s_task;
+  __shared__ __align__(16) float s_fold[kWeighted ? kHubThreads / 32 : 1][128];
   const unsigned rank = cluster.block_rank();
   const int64_t cid = blockIdx.x / kCluster;
   uint32_t *bm = bitmaps + cid * words;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kHubThreads / 32) + wid) * 8 * cap, cap};
+  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kHubThreads / 32) + wid) * 8 * cap, cap,
+                         kWeighted ? s_fold[kWeighted ? wid : 0] : nullptr};
   int32_t *unit_p = cluster.map_shared_rank(&s_unit, 0);
   int32_t *task_p = cluster.map_shared_rank(&s_task, 0);
   const int32_t h0 = cnt[kOffKeys + 0];
