@@ -51,6 +51,22 @@ def byte_model(V, E, sum_min, weighted):
     return b
 
 
+# DRAM bytes (read + write) of one operator call, summed over its kernels, from a one-pass ncu
+# capture of the full-size call (profiles/traffic_rmat24_vc_weighted_unweighted.md).  Keyed by
+# (workload, weighted, edge_centric); other configurations report null.
+MEASURED_TRAFFIC = {
+    ("rmat24w", True, False): 1231537948416,
+    ("rmat24w", False, False): 1043976968192,
+}
+
+
+def l2_note(input_bytes):
+    """How the timed steps relate to the 129 MB L2 (no flush between steps either way)."""
+    if input_bytes > 129e6:
+        return f"inputs ({input_bytes / 1e9:.2f} GB) larger than L2 (129 MB); no flush"
+    return f"inputs ({input_bytes / 1e6:.1f} MB) fit in L2: warm-L2 numbers, no flush"
+
+
 def hbm_peak():
     try:
         with open(PEAKS_FILE) as f:
@@ -688,8 +704,12 @@ def run_gpu(args, world, rank, local):
     B = byte_model(V, E, st["sum_min"], weighted)
     peak, peak_kind = hbm_peak()
     achieved = B / (ms * 1e-3) / 1e9
+    traffic = MEASURED_TRAFFIC.get((args.workload, weighted, bool(args.ec)))
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
+                "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
+                "traffic_note": ("DRAM read+write bytes of one call, one-pass ncu capture of the full-size "
+                                 "call; " + (f"{traffic / (ms * 1e-3) / 1e9:.0f} GB/s of DRAM at this call time"
+                                            if traffic else "not captured for this configuration")),
                 "kernel": "fused operator (one jx_jaccard_ws call = plan, rowsum, sentinel fill, "
                           "hub/CTA/warp row kernels, fix-up)",
                 "algorithmic_bytes": B,
@@ -702,7 +722,7 @@ def run_gpu(args, world, rank, local):
         "data": "synthetic",
         "config": {"workload": f"{args.workload}: {desc}", "algorithm": "edge_centric" if args.ec else "vertex_centric",
                    "weighted": weighted, "V": V, "E": E, "sum_min": st["sum_min"],
-                   "max_degree": st["max_degree"], "l2": "inputs (2.2 GB) larger than L2; no flush",
+                   "max_degree": st["max_degree"], "l2": l2_note(4 * (V + 1) + 4 * E + (4 * V if weighted else 0)),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
         "kernels_ms": kernels,
@@ -785,7 +805,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="jx", choices=["jx", "reference"])
-    ap.add_argument("--workload", default="rmat24w", choices=["rmat24w", "rmat20", "er4096", "batched", "served"])
+    ap.add_argument("--workload", default="rmat24w", choices=["rmat24w", "rmat22w", "rmat20", "er4096", "batched", "served"])
     ap.add_argument("--requests", type=int, default=1000, help="served: requests in the trace")
     ap.add_argument("--rate", type=float, default=2000.0, help="served: Poisson arrival rate (1/s)")
     ap.add_argument("--slots", type=int, default=4, help="served: passes in flight")

@@ -103,6 +103,10 @@ def config_graph(name: str, threads: int = 0):
     if name == "rmat20":
         rp, col = rmat(20, 16, 0.57, 0.19, 0.19, seed=2, threads=threads)
         return rp, col, None, "RMAT scale 20 ef 16 (.57,.19,.19,.05) seed 2, unweighted"
+    if name == "rmat22w":  # the headline shape at a quarter of the size (profiling captures)
+        rp, col = rmat(22, 16, 0.57, 0.19, 0.19, seed=3, threads=threads)
+        w = uniform_weights(len(rp) - 1, seed=4, threads=threads)
+        return rp, col, w, "RMAT scale 22 ef 16 (.57,.19,.19,.05) seed 3, vertex weights U(0,1] seed 4"
     if name == "rmat24w":
         rp, col = rmat(24, 16, 0.57, 0.19, 0.19, seed=3, threads=threads)
         w = uniform_weights(len(rp) - 1, seed=4, threads=threads)
