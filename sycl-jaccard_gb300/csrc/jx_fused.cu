@@ -60,6 +60,7 @@ constexpr int kB1Warps = kRowThreads / 32;
 constexpr int kCap = (kB2Max + 7) / 8; // class-stream capacity per class, B2 (no overflow)
 constexpr int kHubCap = 8192;          // class-stream capacity per class, hubs (overflow resumes)
 constexpr int kHubTasksPerUnit = 32768;
+constexpr int kHubBatch = 2; // tasks a hub-kernel warp takes per fetch (measured best of 32/8/4/2)
 constexpr int kKeys = 128;           // plan sort keys: 4 bins x 32 log2 buckets
 constexpr unsigned kClass0 = 0x01010101u;
 
@@ -828,7 +829,9 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
     for (;;) {
       int32_t k0 = 0, g = 0;
       if (lane == 0) {
-        g = guided_batch(k_end - k_begin - *(volatile int32_t *)task_p, kCluster * (kHubThreads / 32));
+        // hub tasks include whole hub-to-hub intersections: a warp takes at most kHubBatch of them
+        // at a time, so the biggest ones spread over many warps instead of queueing in one
+        g = min(kHubBatch, guided_batch(k_end - k_begin - *(volatile int32_t *)task_p, kCluster * (kHubThreads / 32)));
         k0 = k_begin + atomicAdd(task_p, g);
       }
       k0 = __shfl_sync(kFull, k0, 0);
