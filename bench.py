@@ -55,8 +55,8 @@ def byte_model(V, E, sum_min, weighted):
 # capture of the full-size call (profiles/traffic_rmat24_vc_weighted_unweighted.md).  Keyed by
 # (workload, weighted, edge_centric); other configurations report null.
 MEASURED_TRAFFIC = {
-    ("rmat24w", True, False): 1231537948416,
-    ("rmat24w", False, False): 1043976968192,
+    ("rmat24w", True, False): 1252398987776,
+    ("rmat24w", False, False): 1045355867136,
 }
 
 
