@@ -148,6 +148,28 @@ struct BitmapProbe {
   }
 };
 
+// A hub's neighbour set through a one-hash bit filter of it in shared memory first: most
+// non-members are turned away on chip, and only the rest read the exact bitmap in L2.
+// Filter words per hub CTA (dynamic shared memory).  Measured on R-MAT 24: the unweighted hub
+// kernel drops from 93 to 76 ms with 96 or 192 KB; the weighted one gains nothing (its time is
+// the ordered fold) and loses L1 room for its weight gathers, so it keeps no filter.
+constexpr uint32_t kHubFilterWordsU = 48 * 1024;
+constexpr uint32_t kHubFilterWordsW = 0;
+template <bool kWeighted> __host__ __device__ constexpr uint32_t hub_filter_words() { return kWeighted ? kHubFilterWordsW : kHubFilterWordsU; }
+__device__ __forceinline__ uint32_t filter_bit(int32_t key, uint32_t bits) {
+  return __umulhi((uint32_t)key * 0x9E3779B1u, bits);
+}
+struct FilterProbe {
+  const uint32_t *filt; // shared memory, bits / 32 words
+  const uint32_t *bm;   // global bitmap over [0, n)
+  uint32_t bits;
+  __device__ __forceinline__ bool operator()(int32_t key) const {
+    const uint32_t h = filter_bit(key, bits);
+    if (!((filt[h >> 5] >> (h & 31)) & 1u)) return false;
+    return (__ldcg(bm + (key >> 5)) >> (key & 31)) & 1u;
+  }
+};
+
 // Sorted cur list in global memory (fix-up path).
 struct SearchProbe {
   const int32_t *col;
@@ -788,6 +810,8 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
     const int32_t *__restrict__ unit_off, uint32_t *__restrict__ bitmaps, int64_t words,
     float *__restrict__ out, int32_t *__restrict__ scratch, int cap) {
   cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ uint32_t filt[]; // hub_filter_words(): this CTA's filter of the unit's hub
+  constexpr uint32_t kWords = hub_filter_words<kWeighted>();
   __shared__ int32_t s_unit, s_task;
   __shared__ __align__(16) float s_fold[kWeighted ? kHubThreads / 32 : 1][128];
   const unsigned rank = cluster.block_rank();
@@ -819,12 +843,19 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
     const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
     const int32_t k_begin = (unit - unit_off[lo]) * kHubTasksPerUnit;
     const int32_t k_end = min(du, k_begin + kHubTasksPerUnit);
+    if constexpr (kWords != 0) {
+      for (uint32_t k = threadIdx.x; k < kWords; k += blockDim.x) filt[k] = 0u;
+      __syncthreads();
+      for (int32_t k = threadIdx.x; k < du; k += blockDim.x) { // every CTA filters all of N(u)
+        const uint32_t h = filter_bit(__ldg(col + us + k), kWords * 32);
+        atomicOr(filt + (h >> 5), 1u << (h & 31));
+      }
+    }
     for (int32_t k = rank * blockDim.x + threadIdx.x; k < du; k += kCluster * blockDim.x) {
       const int32_t x = __ldg(col + us + k);
       atomicOr(bm + (x >> 5), 1u << (x & 31));
     }
     cluster.sync();
-    const BitmapProbe probe{bm};
     const float Su = kWeighted ? __ldg(S + u) : 0.0f;
     for (;;) {
       int32_t k0 = 0, g = 0;
@@ -837,7 +868,12 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
       k0 = __shfl_sync(kFull, k0, 0);
       g = __shfl_sync(kFull, g, 0);
       if (k0 >= k_end) break;
-      run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, min(k_end, k0 + g), out);
+      if constexpr (kWords != 0)
+        run_batch<kEC, kWeighted>(FilterProbe{filt, bm, kWords * 32}, cls, row_ptr, col, w, S, u, us, du, Su, k0,
+                                  min(k_end, k0 + g), out);
+      else
+        run_batch<kEC, kWeighted>(BitmapProbe{bm}, cls, row_ptr, col, w, S, u, us, du, Su, k0, min(k_end, k0 + g),
+                                  out);
     }
     cluster.sync();
     for (int32_t k = rank * blockDim.x + threadIdx.x; k < du; k += kCluster * blockDim.x)
@@ -1028,7 +1064,10 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(P.hub_clusters * kCluster);
     cfg.blockDim = dim3(kHubThreads);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = sizeof(uint32_t) * hub_filter_words<kWeighted>();
+    ce = cudaFuncSetAttribute(hub_kernel<kEC, kWeighted>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)cfg.dynamicSmemBytes);
+    if (ce != cudaSuccess) return set_cuda_error(ce);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
