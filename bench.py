@@ -56,7 +56,7 @@ def byte_model(V, E, sum_min, weighted):
 # (workload, weighted, edge_centric); other configurations report null.
 MEASURED_TRAFFIC = {
     ("rmat24w", True, False): 1252398987776,
-    ("rmat24w", False, False): 1045355867136,
+    ("rmat24w", False, False): 1046260130560,
 }
 
 
