@@ -184,7 +184,8 @@ struct SearchProbe {
 // their 4 weights, then the values are added one by one in order through shuffles with
 // constant lane indices, so only the add chain itself is serial.  cap is a multiple of 4, so
 // no int4 read leaves its class.
-template <bool kGlobal> struct Streams {
+template <bool kGlobal, bool kExactCap = false> struct Streams {
+  static constexpr bool kExact = kExactCap; // capacity holds every match: no overflow handling
   int32_t *base;
   int cap;
   float *fbuf = nullptr; // shared memory, 128 floats of this warp for the fold, or none
@@ -230,7 +231,7 @@ template <bool kGlobal> struct Streams {
   }
 };
 template <class S> struct kIsGlobal;
-template <bool G> struct kIsGlobal<Streams<G>> { static constexpr bool value = G; };
+template <bool G, bool E> struct kIsGlobal<Streams<G, E>> { static constexpr bool value = G; };
 
 // All classes at once when none overflowed.  The matched ids are taken in class-major order
 // (class c starts at the prefix sum of the counts of classes < c) 128 per round: lane L holds
@@ -332,7 +333,8 @@ __device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, const 
 }
 
 using ClassStreams = Streams<true>;
-using SmemClassStreams = Streams<false>;
+using ExactClassStreams = Streams<true, true>;
+using SmemClassStreams = Streams<false, true>; // warp-per-row kernel: capacity kB1Max / 8 is exact
 
 // ---------------------------------------------------------------- one task, one warp
 // Class-major strided walk (the reference's order with no buffering); used for overflowing
@@ -431,9 +433,9 @@ __device__ __forceinline__ void task_chunk(const Probe &probe, const int32_t *__
       const unsigned m = __ballot_sync(kFull, f[j]);
       if (f[j]) {
         const int32_t pos = ccount + __popc(m & my_cmask & lt);
-        if (pos < cls.cap) {
+        if (Streams::kExact || pos < cls.cap) {
           cls.put(my_class, pos, x[j]);
-          lastp = base + lane + 32 * j;
+          if (!Streams::kExact) lastp = base + lane + 32 * j;
         }
       }
       ccount += __popc(m & my_cmask);
@@ -465,7 +467,7 @@ __device__ __forceinline__ float task_stream(const Probe &probe, const int32_t *
   if (!kWeighted) return (float)__reduce_add_sync(kFull, cnt);
   __syncwarp();
   float acc = 0.0f;
-  if (!__any_sync(kFull, ccount > cls.cap)) {
+  if (Streams::kExact || !__any_sync(kFull, ccount > cls.cap)) {
     acc = fold_all(cls, lane < 8 ? ccount : 0, w, acc);
     __syncwarp();
     return acc;
@@ -725,8 +727,8 @@ __global__ void __launch_bounds__(kRowThreads) b1_kernel(
 }
 
 // ---------------------------------------------------------------- B2: CTA per row
-template <bool kEC, bool kWeighted, class Probe>
-__device__ __forceinline__ void b2_tasks(const Probe &probe, const ClassStreams &cls, int32_t *s_task,
+template <bool kEC, bool kWeighted, class Probe, class CS>
+__device__ __forceinline__ void b2_tasks(const Probe &probe, const CS &cls, int32_t *s_task,
                                          const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
                                          const float *__restrict__ w, const float *__restrict__ S, int32_t u,
                                          int32_t us, int32_t du, float *__restrict__ out) {
@@ -745,7 +747,7 @@ __device__ __forceinline__ void b2_tasks(const Probe &probe, const ClassStreams 
   }
 }
 
-template <bool kEC, bool kWeighted>
+template <bool kEC, bool kWeighted, bool kExact>
 __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
     const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
@@ -753,7 +755,8 @@ __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
   extern __shared__ int32_t table[];
   __shared__ int32_t s_row, s_task, s_fail;
   const int wid = threadIdx.x >> 5;
-  const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kB2Threads / 32) + wid) * 8 * cap, cap};
+  using CS = Streams<true, kExact>;
+  const CS cls{scratch + ((int64_t)blockIdx.x * (kB2Threads / 32) + wid) * 8 * cap, cap};
   const int32_t r0 = cnt[kOffKeys + 32], r1 = cnt[kOffKeys + 64];
   for (;;) {
     if (threadIdx.x == 0) {
@@ -782,7 +785,7 @@ __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
     }
     // the table uses `slots` words; the last 32 x 128 words of the area, when free, hold the
     // warps' fold buffers
-    ClassStreams rcls = cls;
+    CS rcls = cls;
     if (kWeighted && slots + kB2FoldWords <= (uint32_t)kB2Slots)
       rcls.fbuf = reinterpret_cast<float *>(table + kB2Slots - kB2FoldWords) + wid * 128;
     if (seed < kCuckooSeeds) {
@@ -981,7 +984,9 @@ static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 // GPU; the fixed-scratch entry point uses a small plan whose workspace fits its array.
 Plan default_plan() {
   const int sms = sm_count();
-  return Plan{sms, sms / kCluster > 0 ? sms / kCluster : 1, kCap, kHubCap, sms * 3, sms * 8};
+  Plan P{sms, sms / kCluster > 0 ? sms / kCluster : 1, kCap, kHubCap, sms * 3, sms * 8};
+  P.b2_exact = true; // 8 * kCap >= kB2Max
+  return P;
 }
 
 // Class-stream capacities no larger than a graph can fill: a class of a task holds at most
@@ -994,6 +999,7 @@ Plan fit_plan(Plan P, int64_t e, int64_t max_degree) {
   const int64_t d = std::min<int64_t>(bound, kB2Max);
   const int cap = (int)(((d + 7) / 8 + 3) / 4 * 4);
   P.cap_b2 = std::max(4, std::min(P.cap_b2, cap));
+  P.b2_exact = 8 * (int64_t)P.cap_b2 >= d; // no CTA-bin row exceeds d edges
   if (bound <= kB2Max) P.cap_hub = std::min(P.cap_hub, 4);
   return P;
 }
@@ -1084,10 +1090,19 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
     prof_mark("hub_rows", s);
   }
   const size_t smem_b2 = sizeof(int32_t) * (size_t)kB2Slots;
-  ce = cudaFuncSetAttribute(b2_kernel<kEC, kWeighted>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b2);
-  if (ce != cudaSuccess) return set_cuda_error(ce);
-  b2_kernel<kEC, kWeighted><<<P.b2_ctas, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out,
-                                                                   scratch, P.cap_b2);
+  if (kWeighted && P.b2_exact) {
+    ce = cudaFuncSetAttribute(b2_kernel<kEC, kWeighted, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem_b2);
+    if (ce != cudaSuccess) return set_cuda_error(ce);
+    b2_kernel<kEC, kWeighted, true><<<P.b2_ctas, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt,
+                                                                           out, scratch, P.cap_b2);
+  } else {
+    ce = cudaFuncSetAttribute(b2_kernel<kEC, kWeighted, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem_b2);
+    if (ce != cudaSuccess) return set_cuda_error(ce);
+    b2_kernel<kEC, kWeighted, false><<<P.b2_ctas, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt,
+                                                                            out, scratch, P.cap_b2);
+  }
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("cta_rows", s);
   const size_t smem_b1 = sizeof(int32_t) * (kRowThreads / 32) * (kB1Slots + (kWeighted ? 8 * kB1Cap : 0));

@@ -16,6 +16,9 @@ struct Plan {
   int cap_b2, cap_hub;
   int b1_ctas;      // CTAs of the warp-per-row kernel
   int b0_ctas;      // CTAs of the lane-per-task kernel
+  // cap_b2 holds every match of any CTA-bin task (8 * cap_b2 >= the largest CTA-bin row degree
+  // the graph can have): the CTA kernel then skips the overflow bookkeeping
+  bool b2_exact = false;
 };
 
 Plan default_plan();
