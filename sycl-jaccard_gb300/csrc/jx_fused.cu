@@ -443,6 +443,26 @@ __device__ __forceinline__ void task_chunk(const Probe &probe, const int32_t *__
   }
 }
 
+// Weighted task whose list fits one warp row (dv <= 32): lane k holds position k, gathers its
+// weight when it matches, and the warp adds the matches class by class (lanes c, c+8, c+16,
+// c+24 for class c: the reference's order) straight from registers -- no class streams.
+template <class Probe>
+__device__ __forceinline__ float task_tiny_weighted(const Probe &probe, const int32_t *__restrict__ col,
+                                                    const float *__restrict__ w, int32_t u, int32_t vs,
+                                                    int32_t dv, int32_t &mirror) {
+  const int lane = threadIdx.x & 31;
+  const bool in = lane < dv;
+  const int32_t x = in ? __ldg(col + vs + lane) : 0; // lanes past the list probe vertex 0, a valid key
+  const bool f = probe(x) && in;
+  const float val = f ? __ldg(w + x) : 0.0f;
+  const unsigned m = __ballot_sync(kFull, f);
+  mirror = __reduce_max_sync(kFull, (in && x == u) ? lane : -1);
+  float acc = 0.0f;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) acc = warp_ordered_fold(m & (kClass0 << c), val, acc);
+  return acc;
+}
+
 // Chunked stream of N(v) = col[vs, vs+dv) through `probe`.  Returns the intersection value in
 // the reference's order (count when unweighted) and a position of u in N(v) in `mirror`
 // (-1 absent).  Counts and the position of u are kept per lane and reduced once per task.
@@ -450,6 +470,7 @@ template <bool kWeighted, class Probe, class Streams>
 __device__ __forceinline__ float task_stream(const Probe &probe, const int32_t *__restrict__ col,
                                              const float *__restrict__ w, int32_t u, int32_t vs,
                                              int32_t dv, int32_t &mirror, const Streams &cls) {
+  if (kWeighted && dv <= 32) return task_tiny_weighted(probe, col, w, u, vs, dv, mirror);
   const int lane = threadIdx.x & 31;
   const int my_class = lane & 7;
   int32_t cnt = 0, upos = -1;
