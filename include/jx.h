@@ -38,7 +38,7 @@ typedef enum {
   JX_ERR_CUDA = 2,        /* a CUDA call failed; jx_last_cuda_error() has the code */
   JX_ERR_NOMEM = 3,       /* device or host allocation failed */
   JX_ERR_BAD_GRAPH = 4,   /* jx_csr_check found an invalid CSR */
-  JX_ERR_UNSUPPORTED = 5, /* valid request outside what this build supports */
+  JX_ERR_UNSUPPORTED = 5, /* valid request outside what this library supports */
   JX_ERR_TOO_LARGE = 6    /* size above a documented maximum */
 } jx_status;
 
@@ -171,12 +171,12 @@ jx_status jx_jaccard_list(const jx_csr *g, const float *vertex_w, int64_t num_pa
                           const int32_t *first, const int32_t *second, float *out,
                           jx_stream_t stream);
 
-/* The edge-centric driver's "non zero pairs" count (jaccard.cpp:810-819): *count (device,
+/* The reference's edge-centric driver's "non zero pairs" count (jaccard.cpp:810-819): *count (device,
  * unsigned long long) = number of values[k] > thresh (the reference uses 0.00001). */
 jx_status jx_count_above(int64_t e, const float *values, float thresh, unsigned long long *count,
                          jx_stream_t stream);
 
-/* Reverse-edge removal of the driver's output path (main.cpp:307-309,
+/* Reverse-edge removal of the reference program's output path (main.cpp:307-309,
  * readMtxToCSR.cpp:134-147): keeps (a,b,v) when a > b, or a < b and the reverse edge is absent
  * or holds a different value; drops self loops.  Writes the survivors in CSR order to
  * src/dst/out_values (device, capacity e) and their number to *count (device int64). */

@@ -206,7 +206,7 @@ int jxref_csr_read(const char *path, int32_t *offsets, int32_t *indices, float *
   return 0;
 }
 
-/* The driver's result post-processing (main.cpp:307-309): CSR + per-edge values to an MTX set,
+/* The reference program's result post-processing (main.cpp:307-309): CSR + per-edge values to an MTX set,
  * then removeReverseEdges.  Writes the surviving (src, dst, value) triples (zero-based) in the
  * set's order; returns their number, or -1 when `cap` is too small. */
 int64_t jxref_remove_reverse(int32_t n, int32_t e, const int32_t *offsets, const int32_t *indices,
@@ -235,7 +235,7 @@ int64_t jxref_remove_reverse(int32_t n, int32_t e, const int32_t *offsets, const
   return k;
 }
 
-/* The driver's graph preparation (main.cpp:99-118) on a zero-based edge list: the edges as
+/* The reference program's graph preparation (main.cpp:99-118) on a zero-based edge list: the edges as
  * an MTX set (one-based ids, weight 1), the set's invertDirection inserted when symmetrising,
  * then mtxSetToCSR (self loops dropped unless keep_self).  Writes the CSR's offsets and
  * indices; *nv receives its number of rows (the reference's rows run from the first source to

@@ -345,7 +345,7 @@ def jaccard_list(graph: GraphCSRView, first, second, weights=None, result=None, 
 
 
 def count_above(values, thresh: float = 1e-5, stream=None) -> int:
-    """The edge-centric driver's count of results above `thresh` (jaccard.cpp:810-819)."""
+    """The reference's edge-centric driver (detail::jaccard) count of results above `thresh` (jaccard.cpp:810-819)."""
     torch = _torch()
     c = torch.zeros(1, dtype=torch.int64, device=values.device)
     _check(lib().jx_count_above(values.numel(), _ptr(values, torch.float32, values.numel(), "values"),
@@ -358,7 +358,7 @@ BUILD_KEEP_SELF_LOOPS = 0x2
 
 
 def csr_build(n: int, src, dst, symmetrize: bool = True, keep_self: bool = False, stream=None) -> GraphCSRView:
-    """The driver's graph preparation on the device (main.cpp:99-118, readMtxToCSR.cpp:117-208):
+    """The reference program's graph preparation on the device (main.cpp:99-118, readMtxToCSR.cpp:117-208):
     int32 device edge lists `src`, `dst` (zero-based) -> a CSR with sorted, duplicate-free rows,
     reverse edges added when `symmetrize`, self loops dropped unless `keep_self`."""
     torch = _torch()
@@ -379,7 +379,7 @@ def csr_build(n: int, src, dst, symmetrize: bool = True, keep_self: bool = False
 
 
 def remove_reverse_edges(graph: GraphCSRView, values, stream=None):
-    """The driver's reverse-edge removal before MTX output (main.cpp:307-309): returns the
+    """The reference program's reverse-edge removal before MTX output (main.cpp:307-309): returns the
     surviving (src, dst, value) device tensors in CSR order."""
     torch = _torch()
     E = graph.number_of_edges

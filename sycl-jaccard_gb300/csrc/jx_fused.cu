@@ -998,7 +998,7 @@ __global__ void __launch_bounds__(256) pairs_kernel(int64_t np, const int32_t *_
   }
 }
 
-// ---------------------------------------------------------------- host driver
+// ---------------------------------------------------------------- host side
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Grid sizes and class-stream capacities of one operator call.  The default plan fills the

@@ -1,7 +1,7 @@
 // Result post-processing of the reference's driver, on the device:
 //   - the edge-centric "non zero pairs" count (jaccard.cpp:810-819): values above a threshold;
 //   - reverse-edge removal before MTX output (main.cpp:307-309, readMtxToCSR.cpp:134-147):
-//     the driver turns (row, col, J) into a std::set and, walking it from the largest tuple
+//     the reference program turns (row, col, J) into a std::set and, walking it from the largest tuple
 //     down, erases the reverse (col, row, J) of every tuple still present.  The survivors are
 //     every (a, b) with a > b, and every (a, b) with a < b whose reverse is missing or holds a
 //     different value (equal, or either a NaN -- std::set treats NaN as equivalent); self

@@ -1,4 +1,4 @@
-"""CPU: the binary CSR format (version 2) and the driver's result post-processing against
+"""CPU: the binary CSR format (version 2) and the reference program's result post-processing against
 the reference's own code (readMtxToCSR.cpp, through the host SYCL subset)."""
 import os
 

@@ -1,4 +1,4 @@
-"""GPU: the device CSR builder (the driver's graph preparation) against the oracle's
+"""GPU: the device CSR builder (the reference program's graph preparation) against the oracle's
 restatement, which tests/test_build.py pins to the reference's own set-based code."""
 import ctypes
 

@@ -1,4 +1,4 @@
-"""GPU: the operators next to the path -- pair-list Jaccard, the driver's non-zero count and
+"""GPU: the operators next to the path -- pair-list Jaccard, the reference driver's non-zero count and
 its reverse-edge removal -- against the oracle and the reference's own post-processing."""
 import numpy as np
 import pytest
