@@ -25,9 +25,9 @@
 // Weighted sums follow the reference's accumulation order exactly.  On a CPU SYCL device its
 // 8 i-lanes add their matches one lane after another (jaccard.cpp:343, 370-396): ref
 // positions 0, 8, 16, ..., then 1, 9, 17, ..., i.e. "class" c = position mod 8 major,
-// position minor.  While streaming, the matched values of each class are appended to
+// position minor.  While streaming, the matches' weights of each class are appended to
 // per-warp class streams (shared memory for B1, global scratch otherwise); after the list
-// ends one lane folds them class by class.  A class that outgrows its stream resumes with a
+// ends the warp adds them up class by class.  A class that outgrows its stream resumes with a
 // strided walk over its remaining positions (same order).
 #include "jx_common.cuh"
 #include "jx_plan.h"
@@ -178,12 +178,11 @@ struct SearchProbe {
 };
 
 // ---------------------------------------------------------------- class streams
-// Per-warp storage for the matched vertex ids of the 8 classes (class c at base + c * cap),
-// in ascending ref position.  The weights are gathered only when the warp folds the classes:
-// all lanes load 128 ids at once (one int4 each, the next 128 already in flight) and gather
-// their 4 weights, then the values are added one by one in order through shuffles with
-// constant lane indices, so only the add chain itself is serial.  cap is a multiple of 4, so
-// no int4 read leaves its class.
+// Per-warp class streams of a weighted task: class c's entries from base + c * cap, in
+// ascending ref position.  An entry is the weight of a match (its bit pattern), gathered by
+// vertex id when the match is found, so that the gather's latency overlaps the rest of the
+// chunk and the fold reads the stream alone.  cap is a multiple of 4, so no int4 read leaves
+// its class.
 template <bool kGlobal, bool kExactCap = false> struct Streams {
   static constexpr bool kExact = kExactCap; // capacity holds every match: no overflow handling
   int32_t *base;
@@ -199,8 +198,8 @@ template <bool kGlobal, bool kExactCap = false> struct Streams {
     if (kGlobal) return __ldcg(reinterpret_cast<const int4 *>(p));
     return *reinterpret_cast<const int4 *>(p);
   }
-  // acc = w[x0] + acc, w[x1] + acc, ... over the first n ids of class c; acc uniform.
-  __device__ __forceinline__ float fold(int c, int n, const float *__restrict__ w, float acc) const {
+  // acc = v0 + acc, v1 + acc, ... over the first n entries of class c; acc uniform.
+  __device__ __forceinline__ float fold(int c, int n, float acc) const {
     const int lane = threadIdx.x & 31;
     const int32_t *p = base + c * cap;
     int4 cur = make_int4(0, 0, 0, 0);
@@ -210,10 +209,10 @@ template <bool kGlobal, bool kExactCap = false> struct Streams {
       if (t + 128 + 4 * lane < n) nxt = load4(p + t + 128 + 4 * lane);
       const int k = n - t < 128 ? n - t : 128;
       const int i0 = 4 * lane;
-      const float va = i0 < k ? __ldg(w + cur.x) : 0.0f;
-      const float vb = i0 + 1 < k ? __ldg(w + cur.y) : 0.0f;
-      const float vc = i0 + 2 < k ? __ldg(w + cur.z) : 0.0f;
-      const float vd = i0 + 3 < k ? __ldg(w + cur.w) : 0.0f;
+      const float va = i0 < k ? __int_as_float(cur.x) : 0.0f;
+      const float vb = i0 + 1 < k ? __int_as_float(cur.y) : 0.0f;
+      const float vc = i0 + 2 < k ? __int_as_float(cur.z) : 0.0f;
+      const float vd = i0 + 3 < k ? __int_as_float(cur.w) : 0.0f;
 #pragma unroll
       for (int L = 0; L < 32; ++L) {
         if (4 * L < k) {
@@ -233,11 +232,10 @@ template <bool kGlobal, bool kExactCap = false> struct Streams {
 template <class S> struct kIsGlobal;
 template <bool G, bool E> struct kIsGlobal<Streams<G, E>> { static constexpr bool value = G; };
 
-// All classes at once when none overflowed.  The matched ids are taken in class-major order
+// All classes at once when none overflowed.  The entries are taken in class-major order
 // (class c starts at the prefix sum of the counts of classes < c) 128 per round: lane L holds
-// entries 4L .. 4L+3 of the round and gathers their weights; the ids of the next round are
-// loaded before the current round is folded, so a round waits on one gather, not on an id
-// load and a gather.  The warp then adds the 128 values in order: from a shared-memory copy
+// entries 4L .. 4L+3 of the round; the entries of the next round are loaded before the
+// current round is folded.  The warp then adds the 128 values in order: from a shared-memory copy
 // (one broadcast 16-byte read per 4 values) when the warp has a fold buffer, else through
 // shuffles with constant lane indices; full rounds run without per-value tests.
 // counts: lane c (c < 8) holds class c's count, other lanes 0.  acc uniform.
@@ -247,7 +245,7 @@ template <bool G, bool E> struct kIsGlobal<Streams<G, E>> { static constexpr boo
 template <class S>
 __device__ __forceinline__ int32_t class_entry(const S &cls, const int32_t (&start)[8], const int32_t (&d)[8],
                                                int32_t i, int32_t total) {
-  if (i >= total) return -1;
+  if (i >= total) return 0; // never used: the fold tests the index
   int32_t off = i;
 #pragma unroll
   for (int q = 1; q < 8; ++q) off += i >= start[q] ? d[q] : 0;
@@ -255,8 +253,7 @@ __device__ __forceinline__ int32_t class_entry(const S &cls, const int32_t (&sta
 }
 
 template <class S>
-__device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, const float *__restrict__ w,
-                                          float acc) {
+__device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, float acc) {
   const int lane = threadIdx.x & 31;
   int32_t incl = my_count;
 #pragma unroll
@@ -271,16 +268,16 @@ __device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, const 
   d[0] = 0;
 #pragma unroll
   for (int q = 1; q < 8; ++q) d[q] = cls.cap - (start[q] - start[q - 1]);
-  int32_t id[4];
+  int32_t ent[4];
 #pragma unroll
-  for (int m = 0; m < 4; ++m) id[m] = class_entry(cls, start, d, 4 * lane + m, total);
+  for (int m = 0; m < 4; ++m) ent[m] = class_entry(cls, start, d, 4 * lane + m, total);
   float4 *const buf = reinterpret_cast<float4 *>(cls.fbuf);
   for (int32_t t = 0; t < total; t += 128) {
     float v[4];
 #pragma unroll
-    for (int m = 0; m < 4; ++m) v[m] = id[m] >= 0 ? __ldg(w + id[m]) : 0.0f;
+    for (int m = 0; m < 4; ++m) v[m] = t + 4 * lane + m < total ? __int_as_float(ent[m]) : 0.0f;
 #pragma unroll
-    for (int m = 0; m < 4; ++m) id[m] = class_entry(cls, start, d, t + 128 + 4 * lane + m, total);
+    for (int m = 0; m < 4; ++m) ent[m] = class_entry(cls, start, d, t + 128 + 4 * lane + m, total);
     const int32_t k = total - t < 128 ? total - t : 128;
     if (buf) {
       __syncwarp(); // the previous round's reads are done
@@ -423,6 +420,10 @@ __device__ __forceinline__ void task_chunk(const Probe &probe, const int32_t *__
 #pragma unroll
     for (int j = 0; j < 8; ++j) cnt += f[j];
   } else {
+    // the matches' weights, gathered before the ballots so that the loads overlap them
+    int32_t val[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) val[j] = f[j] ? __float_as_int(__ldg(w + x[j])) : 0;
     // position base + lane + 32j has class (lane & 7); within a class, ascending positions
     // are j-major, lane-minor: the order of these ballots.
     const unsigned lt = (1u << lane) - 1u;
@@ -434,7 +435,7 @@ __device__ __forceinline__ void task_chunk(const Probe &probe, const int32_t *__
       if (f[j]) {
         const int32_t pos = ccount + __popc(m & my_cmask & lt);
         if (Streams::kExact || pos < cls.cap) {
-          cls.put(my_class, pos, x[j]);
+          cls.put(my_class, pos, val[j]);
           if (!Streams::kExact) lastp = base + lane + 32 * j;
         }
       }
@@ -489,13 +490,13 @@ __device__ __forceinline__ float task_stream(const Probe &probe, const int32_t *
   __syncwarp();
   float acc = 0.0f;
   if (Streams::kExact || !__any_sync(kFull, ccount > cls.cap)) {
-    acc = fold_all(cls, lane < 8 ? ccount : 0, w, acc);
+    acc = fold_all(cls, lane < 8 ? ccount : 0, acc);
     __syncwarp();
     return acc;
   }
   for (int c = 0; c < 8; ++c) {
     const int32_t nc = __shfl_sync(kFull, ccount, c);
-    acc = cls.fold(c, nc < cls.cap ? nc : cls.cap, w, acc);
+    acc = cls.fold(c, nc < cls.cap ? nc : cls.cap, acc);
     if (nc > cls.cap) { // resume class c after its last stored value
       const int32_t lp = __reduce_max_sync(kFull, my_class == c ? lastp : -1);
       acc = class_tail(probe, col, w, vs, dv, lp + kIsILanes, acc);
@@ -701,7 +702,7 @@ __device__ __forceinline__ uint32_t cuckoo_slots(int32_t d, uint32_t cap) {
 
 // ---------------------------------------------------------------- B1: warp per row
 // Dynamic shared memory per warp: kB1Slots table slots, then (weighted) 8 * kB1Cap class-stream
-// ids.  (Folds here are short -- at most 512 matches -- and use shuffles, not a fold buffer.)
+// entries.  (Folds here are short -- at most 512 matches -- and use shuffles, not a fold buffer.)
 template <bool kEC, bool kWeighted>
 __global__ void __launch_bounds__(kRowThreads) b1_kernel(
     const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
@@ -1011,7 +1012,7 @@ Plan default_plan() {
 }
 
 // Class-stream capacities no larger than a graph can fill: a class of a task holds at most
-// ceil(d / 8) ids, d the length of the list it walks (<= the maximum degree, <= e), and no row
+// ceil(d / 8) entries, d the length of the list it walks (<= the maximum degree, <= e), and no row
 // of more than kB2Max tasks means no hub units.  Capacities only size buffers (a class that
 // outgrows its buffer resumes from the adjacency list), so a low hint costs speed, not
 // results.  Capacities stay multiples of 4 (int4 reads of a class).
@@ -1181,7 +1182,7 @@ jx_status run_plan(const jx_csr &g, const float *vertex_w, float *out, jx_algo a
 static __device__ __align__(256) unsigned char g_noalloc_scratch[JX_NOALLOC_SCRATCH_BYTES];
 
 // A small grid whose workspace for any graph of at most JX_NOALLOC_MAX_VERTICES vertices fits
-// the array: 8 B2 CTAs, one hub cluster, 1024 ids per class stream (overflows resume).
+// the array: 8 B2 CTAs, one hub cluster, 1024 entries per class stream (overflows resume).
 static Plan noalloc_plan() {
   const int sms = sm_count();
   return Plan{8, 1, 1024, 1024, sms * 3, sms * 8};
