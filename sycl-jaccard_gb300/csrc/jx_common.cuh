@@ -33,6 +33,11 @@ int sm_count();
 // consecutive marks.  A no-op when disabled.
 void prof_mark(const char *name, cudaStream_t s);
 
+// Weighted row sums (jx_rowsum) of the rows of at most max_len entries; longer rows are left to
+// the caller.
+jx_status rowsum_upto(int32_t n, const int32_t *row_ptr, const int32_t *ind, const float *w, float *work,
+                      int32_t max_len, cudaStream_t s);
+
 // -------------------------------------------------------------- device helpers
 
 // Binary search of `key` in col[left .. right] (inclusive), jaccard.cpp:353-367.

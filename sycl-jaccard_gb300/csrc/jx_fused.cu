@@ -601,6 +601,72 @@ __global__ void fill_bits_kernel(int64_t n, uint32_t *__restrict__ x, uint32_t b
     x[i] = bits;
 }
 
+// ---------------------------------------------------------------- row sums of long rows
+// Row sums of the rows of more than kB1Max entries, which the row-sum kernel leaves out, taken
+// from the plan's row lists so that no warp walks several long rows in a row.  The reference's
+// order for a row is T = tree(chunk k) + T over its 32-entry chunks in order
+// (jaccard.cpp:101-119, the tree being lane 31's scan value).  Hub rows (> kB2Max): one CTA
+// per row; the warps reduce the chunks' trees in parallel, 8 chunks per warp at a time, into
+// shared memory, and thread 0 adds the chunk totals in order, kRsSeg chunks per pass.  CTA-bin
+// rows: one warp per row, 8 chunks at a time (independent loads and trees, serial carry).
+constexpr int kRsSeg = 8192;
+__global__ void __launch_bounds__(1024) rowsum_long_kernel(const int32_t *__restrict__ row_ptr,
+                                                           const int32_t *__restrict__ col,
+                                                           const float *__restrict__ w,
+                                                           const int32_t *__restrict__ rows,
+                                                           const int32_t *__restrict__ cnt, float *__restrict__ S) {
+  __shared__ float tot[kRsSeg];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int32_t h0 = cnt[kOffKeys + 0], h1 = cnt[kOffKeys + 32], b2_end = cnt[kOffKeys + 64];
+  for (int32_t i = h0 + blockIdx.x; i < h1; i += gridDim.x) {
+    const int32_t u = rows[i];
+    const int64_t us = __ldg(row_ptr + u);
+    const int64_t du = __ldg(row_ptr + u + 1) - us;
+    const int64_t nch = (du + 31) / 32;
+    float T = 0.0f;
+    for (int64_t c0 = 0; c0 < nch; c0 += kRsSeg) {
+      const int nseg = (int)(nch - c0 < kRsSeg ? nch - c0 : kRsSeg);
+      for (int k = wid * 8; k < nseg; k += (1024 / 32) * 8) {
+        float x[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const int64_t p = (c0 + k + c) * 32 + lane;
+          x[c] = (k + c < nseg && p < du) ? __ldg(w + __ldg(col + us + p)) : 0.0f;
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c) x[c] = warp_tree_sum(x[c]);
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          if (lane == c && k + c < nseg) tot[k + c] = x[c];
+      }
+      __syncthreads();
+      if (threadIdx.x == 0)
+        for (int k = 0; k < nseg; ++k) T = tot[k] + T;
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) S[u] = T;
+  }
+  for (int64_t i = h1 + (int64_t)blockIdx.x * (1024 / 32) + wid; i < b2_end; i += (int64_t)gridDim.x * (1024 / 32)) {
+    const int32_t u = rows[i];
+    const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
+    float T = 0.0f;
+    for (int32_t i0 = 0; i0 < du; i0 += 8 * 32) {
+      float x[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const int32_t p = i0 + 32 * c + lane; // du <= kB2Max: no overflow
+        x[c] = p < du ? __ldg(w + __ldg(col + us + p)) : 0.0f;
+      }
+#pragma unroll
+      for (int c = 0; c < 8; ++c) x[c] = warp_tree_sum(x[c]);
+#pragma unroll
+      for (int c = 0; c < 8; ++c)
+        if (i0 + 32 * c < du) T = x[c] + T; // chunks of the row only
+    }
+    if (lane == 0) S[u] = T;
+  }
+}
+
 // ---------------------------------------------------------------- B0: lane per task
 template <bool kEC, bool kWeighted>
 __global__ void __launch_bounds__(kRowThreads) b0_kernel(
@@ -1081,7 +1147,10 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("plan", s);
   if (kWeighted && !row_sums) {
-    if ((st = jx_rowsum(n, g.e, g.row_ptr, g.col_idx, w, S_ws, (jx_stream_t)s)) != JX_OK) return st;
+    // rows of at most kB1Max entries, then the longer ones from the plan's row lists
+    if ((st = rowsum_upto(n, g.row_ptr, g.col_idx, w, S_ws, kB1Max, s)) != JX_OK) return st;
+    rowsum_long_kernel<<<sms, 1024, 0, s>>>(g.row_ptr, g.col_idx, w, rows, cnt, S_ws);
+    if ((st = check_launch()) != JX_OK) return st;
     prof_mark("rowsum", s);
   }
   fill_bits_kernel<<<sms * 4, 256, 0, s>>>(g.e, reinterpret_cast<uint32_t *>(out), kUnwritten);

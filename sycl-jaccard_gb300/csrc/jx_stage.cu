@@ -16,14 +16,16 @@ namespace jx {
 // A warp takes 32 consecutive rows.  When they hold at most 1024 elements and none is longer
 // than 32, the warp loads their contiguous index span coalesced, gathers the weights into
 // shared memory, and each thread evaluates its own row's tree from there.  Otherwise each
-// short row is loaded by its own thread and rows longer than 32 go to the whole warp.
+// short row is loaded by its own thread and rows longer than 32 go to the whole warp, which
+// loads and reduces 8 chunks at a time (independent loads and trees; only the carry is
+// serial).  Rows of more than max_len entries are skipped (left to the caller).
 constexpr int kRowSumSpan = 1024;
 
 template <bool kWeighted>
 __global__ void __launch_bounds__(256) rowsum_kernel(int32_t n, const int32_t *__restrict__ row_ptr,
                                                       const int32_t *__restrict__ ind,
                                                       const float *__restrict__ w,
-                                                      float *__restrict__ work) {
+                                                      float *__restrict__ work, int32_t max_len) {
   __shared__ float span_buf[kWeighted ? 256 / 32 : 1][kWeighted ? kRowSumSpan : 1];
   const int lane = threadIdx.x & 31;
   float *buf = span_buf[kWeighted ? (threadIdx.x >> 5) : 0];
@@ -57,15 +59,24 @@ __global__ void __launch_bounds__(256) rowsum_kernel(int32_t n, const int32_t *_
       work[r] = x[0] + 0.0f;
     }
     __syncwarp();
-    unsigned longs = __ballot_sync(kFull, r < n && len > 32);
+    unsigned longs = __ballot_sync(kFull, r < n && len > 32 && len <= max_len);
     while (longs) {
       const int b = __ffs(longs) - 1;
       longs &= longs - 1;
       const int32_t sb = __shfl_sync(kFull, start, b), lb = __shfl_sync(kFull, len, b);
       float total = 0.0f;
-      for (int32_t i0 = 0; i0 < lb; i0 += 32) {
-        const float x = (i0 + lane < lb) ? __ldg(w + __ldg(ind + sb + i0 + lane)) : 0.0f;
-        total = warp_tree_sum(x) + total;
+      for (int64_t i0 = 0; i0 < lb; i0 += 8 * 32) {
+        float x[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          const int64_t i = i0 + 32 * c + lane;
+          x[c] = i < lb ? __ldg(w + __ldg(ind + sb + i)) : 0.0f;
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c) x[c] = warp_tree_sum(x[c]);
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          if (i0 + 32 * c < lb) total = x[c] + total; // chunks of the row only
       }
       if (lane == b) work[r] = total;
     }
@@ -197,6 +208,12 @@ static int grid_for(int64_t work_items, int threads, int per_sm = 16) {
   return (int)(want < 1 ? 1 : (want < cap ? want : cap));
 }
 
+jx_status rowsum_upto(int32_t n, const int32_t *row_ptr, const int32_t *ind, const float *w, float *work,
+                      int32_t max_len, cudaStream_t s) {
+  if (n == 0) return JX_OK;
+  rowsum_kernel<true><<<grid_for(n, 256), 256, 0, s>>>(n, row_ptr, ind, w, work, max_len);
+  return check_launch();
+}
 } // namespace jx
 
 using namespace jx;
@@ -210,9 +227,9 @@ jx_status jx_rowsum(int32_t n, int32_t e, const int32_t *row_ptr, const int32_t 
   if (n == 0) return JX_OK;
   cudaStream_t s = (cudaStream_t)stream;
   if (w)
-    rowsum_kernel<true><<<grid_for(n, 256), 256, 0, s>>>(n, row_ptr, ind, w, work);
+    rowsum_kernel<true><<<grid_for(n, 256), 256, 0, s>>>(n, row_ptr, ind, w, work, INT32_MAX);
   else
-    rowsum_kernel<false><<<grid_for(n, 256), 256, 0, s>>>(n, row_ptr, ind, w, work);
+    rowsum_kernel<false><<<grid_for(n, 256), 256, 0, s>>>(n, row_ptr, ind, w, work, INT32_MAX);
   return check_launch();
 }
 

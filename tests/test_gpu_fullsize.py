@@ -78,3 +78,27 @@ def test_weighted_error_vs_fp64(jx, O):
     rel = err / np.maximum(np.abs(J64), 1e-300)
     print(f"weighted RMAT-16 vs FP64: max abs {err.max():.3e}, max rel {rel[J64 > 0].max():.3e}")
     assert rel[J64 > 0].max() < 1e-5
+
+
+def test_hub_row_longer_than_one_rowsum_pass(jx, O):
+    """A hub of 300,000 neighbours -- more than one 8192-chunk pass of the hub-row sum -- whose
+    neighbours form a ring: every edge closes a triangle through the hub, so every weighted J
+    of the graph depends on the hub's row sum.  Bit-exact against the oracle in all modes."""
+    import torch
+    k = 300_000
+    n = k + 1
+    leaves = np.arange(1, k + 1, dtype=np.int64)
+    a = np.concatenate([np.zeros(k, np.int64), leaves[:-1], [k]])
+    b = np.concatenate([leaves, leaves[1:], [1]])
+    key = np.unique(np.concatenate([a * n + b, b * n + a]))
+    rp = np.zeros(n + 1, np.int32)
+    rp[1:] = np.cumsum(np.bincount(key // n, minlength=n))
+    col = (key % n).astype(np.int32)
+    assert rp[1] == k
+    w = jx.graphgen.uniform_weights(n, seed=41)
+    g = jx.GraphCSRView.from_numpy(rp, col)
+    for weights, ec in [(w, False), (None, False), (None, True)]:
+        wt = None if weights is None else torch.from_numpy(weights).cuda()
+        J = jx.jaccard(g, wt, edge_centric=ec).cpu().numpy()
+        want = O.jaccard(rp, col, weights, edge_centric=ec)
+        assert np.array_equal(bits(J), bits(want)), (weights is not None, ec)
