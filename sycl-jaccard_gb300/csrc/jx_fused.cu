@@ -268,6 +268,11 @@ __device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, float 
   d[0] = 0;
 #pragma unroll
   for (int q = 1; q < 8; ++q) d[q] = cls.cap - (start[q] - start[q - 1]);
+  if (total <= 32) { // one entry per lane, added in lane order from registers
+    const float v = lane < total ? __int_as_float(class_entry(cls, start, d, lane, total)) : 0.0f;
+    for (int32_t L = 0; L < total; ++L) acc = __shfl_sync(kFull, v, L) + acc;
+    return acc;
+  }
   int32_t ent[4];
 #pragma unroll
   for (int m = 0; m < 4; ++m) ent[m] = class_entry(cls, start, d, 4 * lane + m, total);
@@ -276,8 +281,10 @@ __device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, float 
     float v[4];
 #pragma unroll
     for (int m = 0; m < 4; ++m) v[m] = t + 4 * lane + m < total ? __int_as_float(ent[m]) : 0.0f;
+    if (t + 128 < total) { // the next round's entries (most tasks have one round)
 #pragma unroll
-    for (int m = 0; m < 4; ++m) ent[m] = class_entry(cls, start, d, t + 128 + 4 * lane + m, total);
+      for (int m = 0; m < 4; ++m) ent[m] = class_entry(cls, start, d, t + 128 + 4 * lane + m, total);
+    }
     const int32_t k = total - t < 128 ? total - t : 128;
     if (buf) {
       __syncwarp(); // the previous round's reads are done
