@@ -739,21 +739,23 @@ __device__ __forceinline__ void run_batch(const Probe &probe, const Streams &cls
                                           float Su, int32_t k0, int32_t k_end, float *__restrict__ out) {
   const int lane = threadIdx.x & 31;
   int32_t v = -1, vs = 0, dv = 0;
+  float Sv = 0.0f; // weighted: S[v], loaded with the degrees rather than after each task
   if (k0 + lane < k_end) {
     v = __ldg(col + us + k0 + lane);
     vs = __ldg(row_ptr + v);
     dv = __ldg(row_ptr + v + 1) - vs;
+    if (kWeighted) Sv = __ldg(S + v);
   }
   unsigned todo = __ballot_sync(kFull, v >= 0 && dv <= du);
   while (todo) {
     const int b = __ffs(todo) - 1;
     todo &= todo - 1;
-    const int32_t tv = __shfl_sync(kFull, v, b), tvs = __shfl_sync(kFull, vs, b),
-                  tdv = __shfl_sync(kFull, dv, b);
+    const int32_t tvs = __shfl_sync(kFull, vs, b), tdv = __shfl_sync(kFull, dv, b);
+    const float tSv = kWeighted ? __shfl_sync(kFull, Sv, b) : 0.0f;
     int32_t mirror;
     const float I = task_stream<kWeighted>(probe, col, w, u, tvs, tdv, mirror, cls);
     if (lane == 0)
-      write_task<kEC, kWeighted>(I, du, tdv, Su, kWeighted ? __ldg(S + tv) : 0.0f, (int64_t)us + k0 + b,
+      write_task<kEC, kWeighted>(I, du, tdv, Su, tSv, (int64_t)us + k0 + b,
                                  mirror >= 0 ? (int64_t)tvs + mirror : -1, out);
   }
 }
