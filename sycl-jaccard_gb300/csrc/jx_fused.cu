@@ -268,9 +268,19 @@ __device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, float 
   d[0] = 0;
 #pragma unroll
   for (int q = 1; q < 8; ++q) d[q] = cls.cap - (start[q] - start[q - 1]);
+  // Values past the total are +0.0 and are added in groups of 4 without tests: acc starts at
+  // +0.0 and a round-to-nearest sum is -0.0 only when both addends are, so acc is never -0.0
+  // and acc + 0.0 is acc bit for bit (a NaN acc is already the canonical NaN).
   if (total <= 32) { // one entry per lane, added in lane order from registers
     const float v = lane < total ? __int_as_float(class_entry(cls, start, d, lane, total)) : 0.0f;
-    for (int32_t L = 0; L < total; ++L) acc = __shfl_sync(kFull, v, L) + acc;
+    for (int32_t L = 0; L < total; L += 4) {
+      const float a = __shfl_sync(kFull, v, L), b = __shfl_sync(kFull, v, L + 1);
+      const float c = __shfl_sync(kFull, v, L + 2), e = __shfl_sync(kFull, v, L + 3);
+      acc = a + acc;
+      acc = b + acc;
+      acc = c + acc;
+      acc = e + acc;
+    }
     return acc;
   }
   int32_t ent[4];
@@ -303,9 +313,9 @@ __device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, float 
         for (int L = 0; 4 * L < k; ++L) {
           const float4 q = buf[L];
           acc = q.x + acc;
-          if (4 * L + 1 < k) acc = q.y + acc;
-          if (4 * L + 2 < k) acc = q.z + acc;
-          if (4 * L + 3 < k) acc = q.w + acc;
+          acc = q.y + acc;
+          acc = q.z + acc;
+          acc = q.w + acc;
         }
       }
     } else if (k == 128) {
@@ -325,9 +335,9 @@ __device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, float 
           const float a = __shfl_sync(kFull, v[0], L), b = __shfl_sync(kFull, v[1], L);
           const float c = __shfl_sync(kFull, v[2], L), e = __shfl_sync(kFull, v[3], L);
           acc = a + acc;
-          if (4 * L + 1 < k) acc = b + acc;
-          if (4 * L + 2 < k) acc = c + acc;
-          if (4 * L + 3 < k) acc = e + acc;
+          acc = b + acc;
+          acc = c + acc;
+          acc = e + acc;
         }
       }
     }

@@ -169,3 +169,22 @@ def test_launch_counter(jx):
     jx.launch_count_reset()
     run(jx, rp, col)
     assert jx.launch_count() >= 3
+
+
+def test_signed_zero_and_infinite_weights(jx, O):
+    """Weights of both signs over seven decades, signed zeros and a few infinities: the engine
+    reproduces the reference's order bit for bit (J = NaN compared as NaN)."""
+    rp, col = jx.graphgen.rmat(16, 16, 0.57, 0.19, 0.19, seed=51)
+    n = len(rp) - 1
+    rng = np.random.default_rng(52)
+    w = (rng.standard_normal(n) * 10.0 ** rng.integers(-3, 4, n)).astype(np.float32)
+    w[rng.random(n) < 0.05] = 0.0
+    w[rng.random(n) < 0.05] = -0.0
+    deg1 = np.flatnonzero(np.diff(rp) == 1)  # infinities on a few leaves, so most J stay finite
+    w[deg1[:3]] = np.inf
+    w[deg1[3:5]] = -np.inf
+    got = run(jx, rp, col, w)
+    want = O.jaccard(rp, col, w)
+    gn, wn = np.isnan(got), np.isnan(want)
+    assert np.array_equal(gn, wn)
+    assert_bitwise(got[~gn], want[~wn], "special weights")
