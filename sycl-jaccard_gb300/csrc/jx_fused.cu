@@ -192,9 +192,6 @@ template <bool kGlobal, bool kExactCap = false> struct Streams {
   __device__ __forceinline__ void put(int c, int pos, int32_t x) const {
     if (kGlobal) __stcg(base + c * cap + pos, x); else base[c * cap + pos] = x;
   }
-  __device__ __forceinline__ int32_t get(int c, int pos) const {
-    return kGlobal ? __ldcg(base + c * cap + pos) : base[c * cap + pos];
-  }
   __device__ __forceinline__ int4 load4(const int32_t *p) const {
     if (kGlobal) return __ldcg(reinterpret_cast<const int4 *>(p));
     return *reinterpret_cast<const int4 *>(p);
@@ -348,7 +345,6 @@ __device__ __forceinline__ float fold_all(const S &cls, int32_t my_count, float 
 }
 
 using ClassStreams = Streams<true>;
-using ExactClassStreams = Streams<true, true>;
 using SmemClassStreams = Streams<false, true>; // warp-per-row kernel: capacity kB1Max / 8 is exact
 
 // ---------------------------------------------------------------- one task, one warp
