@@ -152,8 +152,7 @@ struct BitmapProbe {
 // non-members are turned away on chip, and only the rest read the exact bitmap in L2.
 // Filter words per hub CTA (dynamic shared memory).  Measured on R-MAT 24: the unweighted hub
 // kernel drops from 93 to 76 ms with 96 or 192 KB; the weighted one is slower with any filter
-// (32 / 64 / 192 KB: 197 / 196 / 238 ms against 189 ms without: the filter takes the L1 room
-// its weight gathers and class streams use), so it keeps none.
+// (32 / 64 / 192 KB: 197 / 196 / 238 ms against 189 ms without), so it keeps none.
 constexpr uint32_t kHubFilterWordsU = 48 * 1024;
 constexpr uint32_t kHubFilterWordsW = 0;
 template <bool kWeighted> __host__ __device__ constexpr uint32_t hub_filter_words() { return kWeighted ? kHubFilterWordsW : kHubFilterWordsU; }
