@@ -120,6 +120,23 @@ struct CuckooProbe {
   }
 };
 
+// The cuckoo set with the weight of each key beside it (wt[s] = w[t[s]] for every filled slot
+// s, in shared memory): a weighted lookup returns a match's weight without a global gather.
+struct CuckooWProbe {
+  CuckooProbe c;
+  const float *wt;
+  __device__ __forceinline__ bool operator()(int32_t key) const { return c(key); }
+  __device__ __forceinline__ bool lookup(int32_t key, float &v) const {
+    const uint32_t s1 = c.h1(key), s2 = c.h2(key);
+    const int32_t k1 = c.t[s1], k2 = c.t[s2];
+    const bool f = (k1 == key) | (k2 == key);
+    v = f ? wt[k1 == key ? s1 : s2] : 0.0f;
+    return f;
+  }
+};
+template <class P> struct HasWeights { static constexpr bool value = false; };
+template <> struct HasWeights<CuckooWProbe> { static constexpr bool value = true; };
+
 // Odd multipliers for attempt `seed` (xor with an even number keeps them odd).
 __device__ __forceinline__ CuckooProbe cuckoo_params(const int32_t *t, uint32_t slots, int seed) {
   return CuckooProbe{t, slots / 2, 0x9E3779B1u ^ ((uint32_t)seed * 0x6A09E668u),
@@ -406,8 +423,11 @@ __device__ __forceinline__ void task_chunk(const Probe &probe, const int32_t *__
                                            int32_t dv, int32_t base, const Streams &cls, int32_t &cnt,
                                            int32_t &upos, int32_t &ccount, int32_t &lastp) {
   const int lane = threadIdx.x & 31;
+  // weighted probes that carry the weights: the lookup returns a match's weight
+  constexpr bool kW = kWeighted && HasWeights<Probe>::value;
   int32_t x[8];
   bool f[8];
+  float wv[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
     const int32_t p = base + lane + 32 * j;
@@ -415,15 +435,18 @@ __device__ __forceinline__ void task_chunk(const Probe &probe, const int32_t *__
   }
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
+    wv[j] = 0.0f;
     if (kTail) {
       // rows of the tail past the end of the list (warp-uniform test) probe nothing
       f[j] = false;
       if (base + 32 * j < dv) {
         const int32_t key = x[j] != kEmpty ? x[j] : 0;
-        f[j] = (x[j] != kEmpty) & probe(key);
+        bool hit;
+        if constexpr (kW) hit = probe.lookup(key, wv[j]); else hit = probe(key);
+        f[j] = (x[j] != kEmpty) & hit;
       }
     } else {
-      f[j] = probe(x[j]);
+      if constexpr (kW) f[j] = probe.lookup(x[j], wv[j]); else f[j] = probe(x[j]);
     }
   }
 #pragma unroll
@@ -433,10 +456,11 @@ __device__ __forceinline__ void task_chunk(const Probe &probe, const int32_t *__
 #pragma unroll
     for (int j = 0; j < 8; ++j) cnt += f[j];
   } else {
-    // the matches' weights, gathered before the ballots so that the loads overlap them
+    // the matches' weights (from the probe, or gathered before the ballots so that the loads
+    // overlap them)
     int32_t val[8];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) val[j] = f[j] ? __float_as_int(__ldg(w + x[j])) : 0;
+    for (int j = 0; j < 8; ++j) val[j] = f[j] ? __float_as_int(kW ? wv[j] : __ldg(w + x[j])) : 0;
     // position base + lane + 32j has class (lane & 7); within a class, ascending positions
     // are j-major, lane-minor: the order of these ballots.
     const unsigned lt = (1u << lane) - 1u;
@@ -891,8 +915,28 @@ __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
     CS rcls = cls;
     if (kWeighted && slots + kB2FoldWords <= (uint32_t)kB2Slots)
       rcls.fbuf = reinterpret_cast<float *>(table + kB2Slots - kB2FoldWords) + wid * 128;
+    // weighted rows whose table leaves room: each slot's weight right after the table, below the
+    // fold buffers
+    const bool wtab = kWeighted && seed < kCuckooSeeds && 2 * slots + kB2FoldWords <= (uint32_t)kB2Slots;
+    if (wtab) {
+      float *wt = reinterpret_cast<float *>(table + slots);
+      for (uint32_t k = threadIdx.x; k < slots; k += blockDim.x) {
+        const int32_t key = table[k];
+        wt[k] = key != kEmpty ? __ldg(w + key) : 0.0f;
+      }
+      __syncthreads();
+    }
     if (seed < kCuckooSeeds) {
-      b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), rcls, &s_task, row_ptr, col, w, S, u, us, du, out);
+      if constexpr (kWeighted) {
+        if (wtab) {
+          const CuckooWProbe probe{cuckoo_params(table, slots, seed), reinterpret_cast<const float *>(table + slots)};
+          b2_tasks<kEC, kWeighted>(probe, rcls, &s_task, row_ptr, col, w, S, u, us, du, out);
+        } else {
+          b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), rcls, &s_task, row_ptr, col, w, S, u, us, du, out);
+        }
+      } else {
+        b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), rcls, &s_task, row_ptr, col, w, S, u, us, du, out);
+      }
     } else { // eviction cycles with every multiplier: linear probing (load <= 0.43)
       for (uint32_t k = threadIdx.x; k < slots; k += blockDim.x) table[k] = kEmpty;
       __syncthreads();
