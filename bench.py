@@ -55,7 +55,7 @@ def byte_model(V, E, sum_min, weighted):
 # capture of the full-size call (profiles/traffic_rmat24_vc_weighted_unweighted.md).  Keyed by
 # (workload, weighted, edge_centric); other configurations report null.
 MEASURED_TRAFFIC = {
-    ("rmat24w", True, False): 1251078884608,
+    ("rmat24w", True, False): 1254507681024,
     ("rmat24w", False, False): 1046260130560,
 }
 
