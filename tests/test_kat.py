@@ -56,3 +56,24 @@ def test_isolated_vertices_and_empty(O):
     assert np.allclose(J, 1 / 3) and len(J) == 6
     rp = np.zeros(5, np.int32)
     assert len(O.jaccard(rp, np.zeros(0, np.int32), None)) == 0
+
+
+def test_zero_padding_of_an_ordered_sum():
+    """The engine adds the last partial group of a weighted fold with +0.0 padding.  That is
+    exact: a sequential float32 sum that starts at +0.0 is never -0.0 (round-to-nearest gives
+    -0.0 only for -0.0 + -0.0), so each padding add returns the sum bit for bit -- for weights
+    of both signs, signed zeros, infinities and NaNs alike."""
+    rng = np.random.default_rng(61)
+    pool = np.concatenate([rng.standard_normal(400).astype(np.float32) * np.float32(1e3),
+                           np.float32([0.0, -0.0, np.inf, -np.inf, np.nan, 1e-45, -1e-45])])
+    with np.errstate(invalid="ignore"):  # inf + -inf is part of the domain
+        for _ in range(300):
+            chain = rng.choice(pool, size=int(rng.integers(1, 40)))
+            s = np.float32(0.0)
+            for v in chain:
+                s = np.float32(v + s)
+                assert not (s == 0 and np.signbit(s))
+            padded = s
+            for _ in range(3):
+                padded = np.float32(np.float32(0.0) + padded)
+            assert np.asarray(padded).view(np.uint32) == np.asarray(s).view(np.uint32)
