@@ -251,8 +251,8 @@ template <bool G, bool E> struct kIsGlobal<Streams<G, E>> { static constexpr boo
 // entries 4L .. 4L+3 of the round; the entries of the next round are loaded before the
 // current round is folded.  The warp then adds the 128 values in order: from a shared-memory copy
 // (one broadcast 16-byte read per 4 values) when the warp has a fold buffer, else through
-// shuffles with constant lane indices; full rounds run without per-value tests.
-// counts: lane c (c < 8) holds class c's count, other lanes 0.  acc uniform.
+// shuffles with constant lane indices; values are added in whole groups of 4 (see below).
+// counts: lane c (c < 8) holds class c's count, other lanes 0.  acc: +0.0 on entry.
 //
 // Entry i of class c sits at c * cap + (i - start[c]); with d[q] = cap - count[q - 1] that is
 // i + the sum of d[q] over the classes q >= 1 that start at or before i.
