@@ -52,12 +52,40 @@ def byte_model(V, E, sum_min, weighted):
 
 
 # DRAM bytes (read + write) of one operator call, summed over its kernels, from a one-pass ncu
-# capture of the full-size call (profiles/traffic_rmat24_vc_weighted_unweighted.md).  Keyed by
-# (workload, weighted, edge_centric); other configurations report null.
+# capture (gpu__time_duration, dram__bytes_read/write) of the full-size call.  Keyed by
+# (workload, weighted, edge_centric); each figure carries the fingerprint of the engine sources
+# it was captured on (sources_fingerprint()) and is reported only while the sources match.
 MEASURED_TRAFFIC = {
-    ("rmat24w", True, False): 1254507681024,
-    ("rmat24w", False, False): 1046260130560,
+    ("rmat24w", True, False): (1254507681024, "e1942f32c7573b54"),
+    ("rmat24w", False, False): (1046260130560, "e1942f32c7573b54"),
 }
+
+
+def sources_fingerprint():
+    """sha256 (first 16 hex digits) over the engine's CUDA sources: csrc/*.cu, *.cuh, *.h,
+    each as file name + contents, in name order."""
+    import glob
+    import hashlib
+    d = os.path.join(ROOT, "sycl-jaccard_gb300", "csrc")
+    h = hashlib.sha256()
+    for f in sorted(glob.glob(os.path.join(d, "*.cu")) + glob.glob(os.path.join(d, "*.cuh")) +
+                    glob.glob(os.path.join(d, "*.h"))):
+        h.update(os.path.basename(f).encode())
+        with open(f, "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
+def measured_traffic(key, ms):
+    """(traffic bytes or None, note) for this configuration and the current sources."""
+    if key not in MEASURED_TRAFFIC:
+        return None, "not captured for this configuration"
+    b, fp = MEASURED_TRAFFIC[key]
+    now = sources_fingerprint()
+    if fp != now:
+        return None, f"captured on engine sources {fp}; the sources are now {now}, so it no longer applies"
+    return b, (f"DRAM read+write bytes of one call, one-pass ncu capture of the full-size call on these "
+               f"sources ({fp}); {b / (ms * 1e-3) / 1e9:.0f} GB/s of DRAM at this call time")
 
 
 def l2_note(input_bytes):
@@ -173,96 +201,195 @@ def make_graph(name, threads):
 
 # ------------------------------------------------------------------ CPU reference arm
 
-def sampled_rows(n, K, r):
-    """Rows the reference's IS kernel processes when only work-groups g % K == r run.
-
-    Jaccard_IsKernel::invoke (jaccard.cpp:414-418) uses groups of 8 rows and a grid of
-    min(ceil(n/8), 65535) groups with a row grid-stride, so row x belongs to group
-    ((x mod G0) // 8) with G0 = 8 * min(ceil(n/8), 65535).
-    """
-    G0 = 8 * min((n + 7) // 8, 65535)
-    x = np.arange(n, dtype=np.int64)
-    return ((x % G0) // 8) % K == r
-
-
-def row_work(rp, col):
-    """Per-row cost proxy of the reference's IS kernel: sum over the row's edges of
-    min(d_u, d_v) * (1 + log2(max(d_u, d_v))) (binary searches of the shorter list)."""
-    n = len(rp) - 1
-    d = np.diff(rp.astype(np.int64))
-    work = np.zeros(n, np.float64)
-    step = 1 << 20
-    for s in range(0, n, step):
-        e0, e1 = int(rp[s]), int(rp[min(n, s + step)])
-        du = np.repeat(d[s:min(n, s + step)], d[s:min(n, s + step)])
-        dv = d[col[e0:e1]]
-        c = np.minimum(du, dv) * (1.0 + np.log2(np.maximum(np.maximum(du, dv), 1)))
-        rows = np.repeat(np.arange(s, min(n, s + step)), d[s:min(n, s + step)])
-        work += np.bincount(rows, weights=c, minlength=n)
-    return work
+def makespan(costs, threads):
+    """Duration of one kernel launch of the host SYCL subset in cost units: the first group
+    runs alone (it tells the subset whether the kernel needs fibers), the others are handed
+    in id order to whichever of `threads` threads is free first (OpenMP dynamic schedule)."""
+    import heapq
+    if len(costs) == 0:
+        return 0.0
+    free = [0.0] * threads
+    for c in costs[1:]:
+        heapq.heappush(free, heapq.heappop(free) + float(c))
+    return float(costs[0]) + max(free)
 
 
-def cpu_reference(rp, col, w, target_s=20.0):
-    """Time the reference (through the host SYCL subset) on a bounded work-group sample.
+class RefSampler:
+    """The reference's own kernels (jaccard.cpp through the host SYCL subset) on the host
+    cores, timed on bounded samples of its work-groups and extrapolated to the whole call.
 
-    Fixed per-call cost `a` (the reference allocates 12E + 4V bytes of temporaries per call,
-    jaccard.cpp:931-934) is timed with a sample that runs no work-group.  Then every K-th
-    work-group (residue K/2, evenly spread over the row range through the kernels' grid
-    strides) runs; K is chosen for about target_s seconds.  The whole-graph call time is
-    extrapolated by the sampled share of the IS kernel's work (row_work):
-        T = a + (t_K - a) * W_total / W_sampled,   reported rate = E / T.
-    """
-    from oracle import oracle as O
-    kind = "reference"
-    try:
-        L = O.ref_lib()
-    except Exception as exc:  # build failure on this machine
-        log(f"reference build unavailable: {exc}")
-        L = None
-    threads = os.cpu_count() or 1
-    n, E = len(rp) - 1, len(col)
-    work = row_work(rp, col)
-    W = work.sum()
+    The subset runs each work-group on one thread (its work-items as fibers or a loop), so a
+    call's time is the makespan of its groups over the threads.  Each group's cost is
+    estimated by a proxy (oracle group_work: min(d_u, d_v) * (1 + log2 max) per edge, the
+    binary searches of the dominant kernel, Jaccard_IsKernel or Jaccard_ec_unweighted).  A
+    sample runs, in every kernel of one call, the work-groups that are every K-th in order of
+    cost (stratified: R-MAT degrees follow the bits of the vertex id, so a stride over group
+    ids would pick groups of one cost level); with `a` the fixed per-call cost (a call that
+    runs no group: the reference's per-call temporaries, jaccard.cpp:931-934) and t the
+    sample's time, the seconds per cost unit are c = (t - a) / makespan(sample), and the whole
+    call takes T = a + c * makespan(all groups).  A light calibration sample gives a first c;
+    each step's sample then holds about one group per thread from the heaviest stratum whose
+    predicted duration fits the target, at successive offsets, and gives its own c and T.  Without the reference build, the C
+    restatement (kind "port") is timed on row ranges and extrapolated by work share."""
 
-    def timed(K, r):
-        t0 = time.perf_counter()
-        if kind == "reference":
-            O.ref_jaccard(rp, col, w, edge_centric=False, threads=threads, group_sample=K, group_residue=r)
+    def __init__(self, rp, col, w, edge_centric=False, threads=None):
+        from oracle import oracle as O
+        self.O = O
+        self.rp, self.col, self.w, self.ec = rp, col, w, edge_centric
+        self.n, self.E = len(rp) - 1, len(col)
+        self.threads = threads or os.cpu_count() or 1
+        try:
+            self.L = O.ref_lib()
+        except Exception as exc:  # build failure on this machine
+            log(f"reference build unavailable: {exc}")
+            self.L = None
+        self.kind = "reference" if self.L is not None else "port"
+        self.spent = 0.0
+        self.calls = 0
+        self.c = None
+        if self.kind == "reference":
+            self.gw = O.group_work(rp, col, edge_centric, self.threads)
+            self.order = np.argsort(-self.gw, kind="stable")
+            self.M_full = makespan(self.gw, self.threads)
+            self.a = self._run(np.zeros(len(self.gw), np.uint8))
         else:
-            rows = (r, min(n, r + max(1, n // K)))
-            O.jaccard(rp, col, w, rows=rows, threads=threads)
-        return time.perf_counter() - t0
+            self.rw = O.row_work(rp, col, self.threads)
+            self.K_max = max(1, self.n // (8 * self.threads))
+            self.W = float(self.rw.sum()) or 1.0
+            self.a = 0.0
 
-    if L is None:
-        kind = "port"
-    if kind == "reference":
-        a = timed(1 << 40, (1 << 40) - 1)
-        share = lambda K: work[sampled_rows(n, K, K // 2)].sum() / W
+    def _ids(self, K, offset):
+        return np.sort(self.order[offset % K::K])
+
+
+    def _model(self, K, offset):
+        """(what to run, cost units of the sample: its makespan, or its work share for a port)."""
+        if self.kind == "reference":
+            ids = self._ids(K, offset)
+            mask = np.zeros(len(self.gw), np.uint8)
+            mask[ids] = 1
+            return mask, makespan(self.gw[ids], self.threads)
+        size = max(1, self.n // K)
+        lo = (offset * size) % max(1, self.n - size + 1)
+        return (lo, min(self.n, lo + size)), float(self.rw[lo:lo + size].sum()) / self.W
+
+    def _run(self, what):
+        t0 = time.perf_counter()
+        if self.kind == "reference":
+            self.O.ref_jaccard(self.rp, self.col, self.w, edge_centric=self.ec, threads=self.threads,
+                               group_mask=what)
+        else:
+            self.O.jaccard(self.rp, self.col, self.w, edge_centric=self.ec, rows=what, threads=self.threads)
+        t = time.perf_counter() - t0
+        self.spent += t
+        return t
+
+    def _full_units(self):
+        return self.M_full if self.kind == "reference" else 1.0
+
+    def _step_choice(self, target_s):
+        """(K, offset) of a sample predicted to take about target_s seconds: one group per thread
+        (K = groups / threads) from the heaviest offset that fits the target; denser samples
+        when even offset 0 fits (small graphs)."""
+        if self.kind != "reference":
+            return int(min(self.n, max(1, round(1.0 / max(target_s / max(self.c, 1e-12), 1e-12))))), self.calls
+        G = len(self.gw)
+        pred = lambda K, off: self.a + self.c * self._model(K, off)[1]
+        Ks = max(1, G // self.threads)
+        if pred(Ks, 0) <= target_s:  # even the heaviest groups fit: make the sample denser
+            lo, hi = 1, Ks
+            while lo < hi:
+                mid = (lo + hi) // 2
+                if pred(mid, 0) <= target_s:
+                    hi = mid
+                else:
+                    lo = mid + 1
+            return lo, self.calls % lo
+        lo, hi = 0, Ks - 1  # the lowest offset (heaviest groups) predicted to fit the target
+        while lo < hi:
+            mid = (lo + hi) // 2
+            if pred(Ks, mid) <= target_s:
+                hi = mid
+            else:
+                lo = mid + 1
+        return Ks, (lo + self.calls) % Ks
+
+    def sample(self, target_s):
+        """One sample of about target_s seconds; returns (extrapolated whole-call seconds,
+        details).  The first call also runs the calibration sample."""
+        if self.c is None:  # calibration: a light sample, one group per thread
+            K = self.K_max if self.kind != "reference" else max(1, len(self.gw) // self.threads)
+            off = K - 1 if self.kind == "reference" else K // 2
+            what, units = self._model(K, off)
+            t = self._run(what)
+            self.c = max(t - self.a, 1e-4) / max(units, 1e-12)
+            self.calib = {"K": K, "offset": off, "sample_s": round(t, 3),
+                          "call_s": round(self.a + self.c * self._full_units(), 2)}
+        K, offset = self._step_choice(target_s)
+        what, units = self._model(K, offset)
+        t = self._run(what)
+        self.calls += 1
+        self.c = max(t - self.a, 1e-6) / max(units, 1e-12)
+        T = self.a + self.c * self._full_units()
+        info = {"K": K, "offset": offset, "sample_s": t, "units": units}
+        if self.kind == "reference":
+            ids = self._ids(K, offset)
+            info["groups"] = len(ids)
+            info["share"] = float(self.gw[ids].sum() / self.gw.sum())
+            info["parallel_eff"] = float(self.gw[ids].sum() / self.threads / max(units, 1e-12))
+        return T, info
+
+    def describe(self, info, weighted):
+        algo = "EC" if self.ec else f"VC{' weighted' if weighted else ''}"
+        if self.kind == "reference":
+            return (f"reference jaccard.cpp ({algo}) via host SYCL subset, {self.threads} threads: in every kernel "
+                    f"of one call the work-groups that are every {info['K']}-th of the {len(self.gw)} in order of "
+                    f"cost from offset {info['offset']} ({info['groups']} groups, {info['share']:.2e} of the "
+                    f"{'EC' if self.ec else 'IS'} kernel's work, parallel efficiency {info['parallel_eff']:.2f}); "
+                    f"fixed per-call cost {self.a:.2f}s + sampled {info['sample_s'] - self.a:.2f}s, extrapolated "
+                    f"by the makespan of the groups' cost proxy over the threads (whole call: efficiency "
+                    f"{self.gw.sum() / self.threads / self.M_full:.3f}); light calibration sample "
+                    f"{self.calib['sample_s']}s, whole call {self.calib['call_s']}s")
+        return f"C restatement (oracle port), a row range with {info['units']:.2e} of the work, {self.threads} threads"
+
+
+def cpu_reference(rp, col, w, target_s=20.0, edge_centric=False):
+    """The reference on this machine's host cores: one bounded sample of about target_s seconds
+    (RefSampler), reported as edges per second of the extrapolated whole call."""
+    s = RefSampler(rp, col, w, edge_centric)
+    T, info = s.sample(target_s)
+    return {"value": s.E / T, "unit": UNIT, "cores": s.threads, "kind": s.kind,
+            "sample": s.describe(info, w is not None), "seconds": round(s.spent, 3),
+            "extrapolated_call_s": round(T, 2)}
+
+
+def oracle_parity(rp, col, w, edge_centric, got):
+    """The engine's results checked against the oracle (the C restatement, pinned bit for bit to
+    the reference) -- on the whole graph when it is small, else on the sampled row ranges of
+    oracle.check_rows (largest hubs, a CTA-size row, a middle band, the tail)."""
+    from oracle import oracle as O
+    got = np.ascontiguousarray(got, np.float32).view(np.uint32)
+    threads = os.cpu_count() or 1
+    t0 = time.time()
+    n, E = len(rp) - 1, len(col)
+    if E <= 5_000_000:
+        ranges = [("all", 0, n)]
     else:
-        a = 0.0
-        share = lambda K: work[K // 2: min(n, K // 2 + max(1, n // K))].sum() / W
-    K = 4096
-    t_cal = timed(K, K // 2)
-    full = max(t_cal - a, 1e-4) / max(share(K), 1e-12)
-    K = 1
-    while K < (1 << 20) and full * share(K * 2) >= target_s:
-        K *= 2
-    while K > 1 and full * share(K) < target_s / 2:
-        K //= 2
-    t = timed(K, K // 2)
-    sh = share(K)
-    T = a + max(t - a, 1e-6) / max(sh, 1e-12)
-    if kind == "reference":
-        sel = sampled_rows(n, K, K // 2)
-        edges = int(np.diff(rp.astype(np.int64))[sel].sum())
-        sample = (f"reference jaccard.cpp (VC{' weighted' if w is not None else ''}) via host SYCL "
-                  f"subset, work-groups g % {K} == {K // 2} of each kernel ({edges} of {E} edges, "
-                  f"{sh:.2e} of the IS work), {threads} threads; fixed per-call cost {a:.2f}s + "
-                  f"sampled {t - a:.2f}s, extrapolated to the whole graph by work share")
-    else:
-        sample = f"C restatement (oracle port), a row range with {sh:.2e} of the work, {threads} threads"
-    return {"value": E / T, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample,
-            "seconds": round(a + t + t_cal, 3), "extrapolated_call_s": round(T, 2)}
+        ranges = O.check_rows(rp)
+    S = O.rowsum(rp, col, w, threads) if (w is not None and not edge_centric) else None
+    bad, edges, names = 0, 0, []
+    for name, r0, r1 in ranges:
+        if S is not None:
+            want = O.jaccard_rows_with_sums(rp, col, w, S, (r0, r1), threads)
+        else:
+            want = O.jaccard(rp, col, None, edge_centric=edge_centric, rows=(r0, r1), threads=threads)
+        lo, hi = int(rp[r0]), int(rp[r1])
+        bad += int((got[lo:hi] != want.view(np.uint32)).sum())
+        edges += hi - lo
+        names.append(name)
+    return {"result": ("bit-exact" if bad == 0 else f"{bad} mismatches") + f" on {edges} edges",
+            "mismatches": bad, "edges_checked": edges, "rows": names,
+            "oracle": "C restatement of jaccard.cpp, pinned to the reference", "seconds": round(time.time() - t0, 2)}
 
 
 # ------------------------------------------------------------------ batched workload
@@ -295,27 +422,38 @@ def super_batches(st):
     return groups
 
 
+class BatchRefSampler:
+    """The reference on the host cores over a stratified sample of a list of graphs: 8 graphs
+    evenly spaced in edge-count order, each with its own RefSampler.  A sample times every
+    picked graph once (target_s split between them); the rate is (sum of their edges) / (sum
+    of their extrapolated call times).  weights: per-graph vertex weights (weighted VC) or
+    None (unweighted VC)."""
+
+    def __init__(self, graphs, st, weights=None, what="graphs of the batch"):
+        order = np.argsort([x["E"] for x in st], kind="stable")
+        self.pick = [int(order[int(q)]) for q in np.linspace(0, len(order) - 1, 8)]
+        self.samplers = [RefSampler(graphs[i][0], graphs[i][1], None if weights is None else weights[i])
+                         for i in self.pick]
+        self.E = float(sum(st[i]["E"] for i in self.pick))
+        self.weighted = weights is not None
+        self.what = what
+
+    def sample(self, target_s):
+        T = sum(s.sample(target_s / len(self.samplers))[0] for s in self.samplers)
+        return T
+
+    def result(self, T):
+        s0 = self.samplers[0]
+        return {"value": self.E / T, "unit": UNIT, "cores": s0.threads, "kind": s0.kind,
+                "sample": f"reference jaccard.cpp (VC{' weighted' if self.weighted else ''}) on 8 {self.what} "
+                          f"evenly spaced in edge count ({int(self.E)} edges), each on a work-group sample "
+                          f"extrapolated to its whole call; rate = sum of edges / sum of call times",
+                "seconds": round(sum(s.spent for s in self.samplers), 3), "extrapolated_call_s": round(T, 3)}
+
+
 def cpu_reference_batch(graphs, st, target_s=20.0, weights=None, what="graphs of the batch"):
-    """Reference on the host cores over a stratified sample of a list of graphs: 8 graphs
-    evenly spaced in edge-count order, each timed with cpu_reference's work-group sampling; the
-    rate is (sum of their edges) / (sum of their extrapolated call times).  weights: per-graph
-    vertex weights (weighted VC) or None (unweighted VC)."""
-    order = np.argsort([x["E"] for x in st], kind="stable")
-    pick = [int(order[int(q)]) for q in np.linspace(0, len(order) - 1, 8)]
-    E = T = 0.0
-    threads, kind = None, None
-    for i in pick:
-        rp, col = graphs[i][0], graphs[i][1]
-        cb = cpu_reference(rp, col, None if weights is None else weights[i], target_s / len(pick))
-        E += st[i]["E"]
-        T += cb["extrapolated_call_s"]
-        threads, kind = cb["cores"], cb["kind"]
-    return {"value": E / T, "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": f"reference jaccard.cpp (VC{' weighted' if weights is not None else ''}) on 8 {what} "
-                      f"evenly spaced in edge count "
-                      f"({int(E)} edges), each on a work-group sample extrapolated to its whole call; "
-                      f"rate = sum of edges / sum of call times",
-            "extrapolated_call_s": round(T, 3)}
+    b = BatchRefSampler(graphs, st, weights, what)
+    return b.result(b.sample(target_s))
 
 
 def run_gpu_batched(args, world, rank, local):
@@ -638,6 +776,52 @@ def run_gpu_served(args, world, rank, local):
 
 # ------------------------------------------------------------------ GPU arm
 
+def time_calls(jx, world, local, stream, call, steps, warmup):
+    """W untimed calls, then `steps` calls between barrier + synchronize, CUDA events on the
+    launching stream; returns (ms per call, max over ranks), kernels launched, clock summary."""
+    import torch
+    for _ in range(warmup):
+        call()
+    torch.cuda.synchronize()
+    barrier(world)
+    torch.cuda.synchronize()
+    jx.launch_count_reset()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(steps):
+            call()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = jx.launch_count()
+    barrier(world)
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / steps, world)
+    return ms, launches, clk.summary()
+
+
+def copy_rates(V, E, weighted):
+    """Host<->device copy rates of this machine for the e2e arrays (pinned host memory, one
+    cudaMemcpyAsync per array, CUDA events): GB/s for H2D of row_ptr + col (+ w) and D2H of J."""
+    import torch
+    h_in = torch.empty(4 * (V + 1) + 4 * E + (4 * V if weighted else 0), dtype=torch.uint8).pin_memory()
+    h_out = torch.empty(4 * E, dtype=torch.uint8).pin_memory()
+    d_in = torch.empty(h_in.numel(), dtype=torch.uint8, device="cuda")
+    d_out = torch.empty(h_out.numel(), dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream()
+    res = {}
+    for name, dst, src in (("h2d", d_in, h_in), ("d2h", h_out, d_out)):
+        dst.copy_(src, non_blocking=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(3):
+            dst.copy_(src, non_blocking=True)
+        e1.record(s)
+        torch.cuda.synchronize()
+        res[name + "_gbs"] = round(3 * src.numel() / (e0.elapsed_time(e1) * 1e-3) / 1e9, 1)
+    del h_in, h_out, d_in, d_out
+    return res
+
+
 def run_gpu(args, world, rank, local):
     import torch
     jx = importlib.import_module("sycl-jaccard_gb300")
@@ -647,7 +831,6 @@ def run_gpu(args, world, rank, local):
     if args.unweighted:
         w, desc = None, desc + " (weights dropped: unweighted)"
     elif args.weighted and w is None:
-        jx = importlib.import_module("sycl-jaccard_gb300")
         w = jx.graphgen.uniform_weights(st["V"], seed=4, threads=threads)
         desc += " + vertex weights U(0,1] seed 4"
     V, E = st["V"], st["E"]
@@ -658,28 +841,13 @@ def run_gpu(args, world, rank, local):
     ws = torch.empty(jx.workspace_size(g, weighted, args.ec), dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
 
-    for _ in range(args.warmup):
-        jx.jaccard(g, wd, out, edge_centric=args.ec, workspace=ws)
-    torch.cuda.synchronize()
-    barrier(world)
-    torch.cuda.synchronize()
-    jx.launch_count_reset()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clk:
-        ev0.record(stream)
-        for _ in range(args.steps):
-            jx.jaccard(g, wd, out, edge_centric=args.ec, workspace=ws)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-    launches = jx.launch_count()
-    barrier(world)
-    ms = ev0.elapsed_time(ev1) / args.steps
-    ms = max_over_ranks(ms, world)
-    clocks = clk.summary()
+    call = lambda: jx.jaccard(g, wd, out, edge_centric=args.ec, workspace=ws)
+    ms, launches, clocks = time_calls(jx, world, local, stream, call, args.steps, args.warmup)
+    result_bits = out.cpu().numpy().copy()
 
     # per-launch breakdown of one extra (untimed) step
     jx.lib().jx_profile_begin()
-    jx.jaccard(g, wd, out, edge_centric=args.ec, workspace=ws)
+    call()
     buf = ctypes.create_string_buffer(4096)
     jx.lib().jx_profile_end(buf, 4096)
     kernels = {}
@@ -699,15 +867,15 @@ def run_gpu(args, world, rank, local):
         h_out = torch.empty(E, dtype=torch.float32).pin_memory()
         L = jx.lib()
         algo = 1 if args.ec else 0
-        call = lambda: L.jx_jaccard_host(V, E, h_rp.data_ptr(), h_col.data_ptr(),
-                                         h_w.data_ptr() if h_w is not None else None,
-                                         h_out.data_ptr(), algo)
+        host_call = lambda: L.jx_jaccard_host(V, E, h_rp.data_ptr(), h_col.data_ptr(),
+                                              h_w.data_ptr() if h_w is not None else None,
+                                              h_out.data_ptr(), algo)
         for _ in range(min(2, args.warmup)):
-            assert call() == 0
+            assert host_call() == 0
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
-            rc = call()
+            rc = host_call()
             assert rc == 0, rc
         t1 = time.perf_counter()
         e2e_s = (t1 - t0) / args.e2e_steps
@@ -716,20 +884,19 @@ def run_gpu(args, world, rank, local):
         e2e = {"value": E * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": 4 * E, "ms_per_step": round(e2e_s * 1e3, 3),
                "timing": "host wall clock around the synchronous call"}
-        out_host = h_out.numpy()
-        dev = out.cpu().numpy()
-        if not np.array_equal(out_host.view(np.uint32), dev.view(np.uint32)):
+        e2e.update(copy_rates(V, E, weighted))
+        e2e["copy_ms_at_these_rates"] = round(h2d / e2e["h2d_gbs"] / 1e6 + 4 * E / e2e["d2h_gbs"] / 1e6, 2)
+        if not np.array_equal(h_out.numpy().view(np.uint32), result_bits.view(np.uint32)):
             raise AssertionError("host-buffer entry point disagrees with the device path")
+        del h_rp, h_col, h_w, h_out
 
     B = byte_model(V, E, st["sum_min"], weighted)
     peak, peak_kind = hbm_peak()
     achieved = B / (ms * 1e-3) / 1e9
-    traffic = MEASURED_TRAFFIC.get((args.workload, weighted, bool(args.ec)))
+    traffic, traffic_note = measured_traffic((args.workload, weighted, bool(args.ec)), ms)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "peak_source": peak_kind,
-                "traffic_note": ("DRAM read+write bytes of one call, one-pass ncu capture of the full-size "
-                                 "call; " + (f"{traffic / (ms * 1e-3) / 1e9:.0f} GB/s of DRAM at this call time"
-                                            if traffic else "not captured for this configuration")),
+                "traffic_source": traffic_note, "sources": sources_fingerprint(),
                 "kernel": "fused operator (one jx_jaccard_ws call = plan, rowsum, sentinel fill, "
                           "hub/CTA/warp row kernels, fix-up)",
                 "algorithmic_bytes": B,
@@ -747,76 +914,87 @@ def run_gpu(args, world, rank, local):
         "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
         "kernels_ms": kernels,
     }
+
+    # the same graph unweighted (vertex-centric): a few more timed calls, reported beside
+    unw_bits = None
+    if weighted and not args.no_unweighted:
+        call_u = lambda: jx.jaccard(g, None, out, edge_centric=False, workspace=ws)
+        ms_u, _, clk_u = time_calls(jx, world, local, stream, call_u, 5, 2)
+        unw_bits = out.cpu().numpy()
+        B_u = byte_model(V, E, st["sum_min"], False)
+        result["unweighted"] = {"ms_per_step": round(ms_u, 4), "value": E * world / (ms_u * 1e-3), "unit": UNIT,
+                                "steps": 5, "warmup": 2, "algorithmic_bytes": B_u,
+                                "frac": round(B_u / (ms_u * 1e-3) / 1e9 / peak, 4), "clocks": clk_u}
+
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
-            result["cpu_baseline"] = cpu_reference(rp, col, w if weighted else None, args.cpu_seconds)
+            result["cpu_baseline"] = cpu_reference(rp, col, w if weighted else None, args.cpu_seconds, args.ec)
         except Exception as exc:
             result["cpu_baseline"] = {"value": None, "error": str(exc)[:200]}
+        try:
+            result["parity"] = oracle_parity(rp, col, w if weighted else None, args.ec, result_bits)
+            if unw_bits is not None:
+                result["unweighted"]["parity"] = oracle_parity(rp, col, None, False, unw_bits)
+        except Exception as exc:
+            result["parity"] = {"result": None, "error": str(exc)[:200]}
     return result
 
 
 def run_reference(args, world, rank):
+    """The reference arm: the reference's own kernels on this machine's host cores, all
+    threads.  Set-up (graph, work model, calibration) happens once; then one untimed warm-up
+    sample (when warmup > 0) and `steps` samples of about ref_seconds / steps seconds each,
+    on successive work-group residues.  The value is E / the median extrapolated call time."""
     if rank != 0:
         return None
     threads = os.cpu_count() or 1
-    if args.workload == "served":
-        jx = importlib.import_module("sycl-jaccard_gb300")
-        res, up, st_res, st_up = make_served(threads)
-        _, trace_g = jx.graphgen.poisson_trace(args.requests, args.rate, len(res), len(up), seed=6)
-        pick = [(res if k == "resident" else up)[i] for k, i in trace_g]
-        pst = [(st_res if k == "resident" else st_up)[i] for k, i in trace_g]
-        vals, cb = [], None
-        for i in range(args.warmup + args.steps):
-            cb = cpu_reference_batch(pick, pst, args.cpu_seconds / max(1, args.steps),
-                                     weights=[g[2] for g in pick], what="requests of the trace")
-            if i >= args.warmup:
-                vals.append(cb["value"])
-        value = statistics.median(vals)
-        cb["value"] = value
-        return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "impl": "reference",
-                "config": {"workload": f"served: {args.requests} requests (see the jx arm), serial reference calls",
-                           "algorithm": "vertex_centric", "weighted": True},
-                "cpu_baseline": cb,
-                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    if args.workload == "batched":
-        graphs, st = make_batch(threads)
-        vals, cb = [], None
-        for i in range(args.warmup + args.steps):
-            cb = cpu_reference_batch(graphs, st, args.cpu_seconds / max(1, args.steps))
-            if i >= args.warmup:
-                vals.append(cb["value"])
-        value = statistics.median(vals)
-        cb["value"] = value
-        E = sum(x["E"] for x in st)
-        return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": round(E / value * 1e3, 3), "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "impl": "reference",
-                "config": {"workload": "batched: 2000 graphs seed 5 (see the jx arm)", "algorithm": "vertex_centric",
-                           "graphs": len(graphs), "E": E},
-                "cpu_baseline": cb,
-                "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    per = max(0.5, args.ref_seconds / max(1, args.steps))
+    common = {"metric": METRIC, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+              "data": "synthetic", "impl": "reference"}
+    if args.workload in ("served", "batched"):
+        if args.workload == "served":
+            jx = importlib.import_module("sycl-jaccard_gb300")
+            res, up, st_res, st_up = make_served(threads)
+            _, trace_g = jx.graphgen.poisson_trace(args.requests, args.rate, len(res), len(up), seed=6)
+            pick = [(res if k == "resident" else up)[i] for k, i in trace_g]
+            pst = [(st_res if k == "resident" else st_up)[i] for k, i in trace_g]
+            bs = BatchRefSampler(pick, pst, weights=[g[2] for g in pick], what="requests of the trace")
+            config = {"workload": f"served: {args.requests} requests (see the jx arm), serial reference calls",
+                      "algorithm": "vertex_centric", "weighted": True}
+        else:
+            graphs, st = make_batch(threads)
+            bs = BatchRefSampler(graphs, st)
+            config = {"workload": "batched: 2000 graphs seed 5 (see the jx arm)", "algorithm": "vertex_centric",
+                      "graphs": len(graphs), "E": sum(x["E"] for x in st)}
+        if args.warmup > 0:
+            bs.sample(per)
+        Ts = [bs.sample(per) for _ in range(args.steps)]
+        cb = bs.result(statistics.median(Ts))
+        value = cb["value"]
+        return dict(common, value=value, ms_per_step=round(bs.E / value * 1e3, 3), config=config,
+                    cpu_baseline=cb,
+                    e2e={"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
     rp, col, w, desc, st = make_graph(args.workload, threads)
     weighted = w is not None and not args.ec
-    vals = []
-    cb = None
-    for i in range(args.warmup + args.steps):
-        cb = cpu_reference(rp, col, w if weighted else None, args.cpu_seconds / max(1, args.steps))
-        if i >= args.warmup:
-            vals.append(cb["value"])
-    value = statistics.median(vals)
-    cb["value"] = value
-    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(st["E"] / value * 1e3, 3),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "impl": "reference",
-            "config": {"workload": f"{args.workload}: {desc}", "algorithm": "vertex_centric",
-                       "weighted": weighted, "V": st["V"], "E": st["E"], "sum_min": st["sum_min"]},
-            "cpu_baseline": cb,
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    sm = RefSampler(rp, col, w if weighted else None, edge_centric=args.ec, threads=threads)
+    if args.warmup > 0:
+        sm.sample(per)
+    runs = [sm.sample(per) for _ in range(args.steps)]
+    Ts = [T for T, _ in runs]
+    Tm = statistics.median(Ts)
+    value = st["E"] / Tm
+    info = runs[len(runs) // 2][1]
+    cb = {"value": value, "unit": UNIT, "cores": sm.threads, "kind": sm.kind,
+          "sample": sm.describe(info, weighted) + f"; median of {len(Ts)} samples at successive offsets",
+          "seconds": round(sm.spent, 3), "extrapolated_call_s": round(Tm, 2),
+          "extrapolated_call_s_range": [round(min(Ts), 2), round(max(Ts), 2)]}
+    return dict(common, value=value, ms_per_step=round(Tm * 1e3, 3),
+                config={"workload": f"{args.workload}: {desc}",
+                        "algorithm": "edge_centric" if args.ec else "vertex_centric",
+                        "weighted": weighted, "V": st["V"], "E": st["E"], "sum_min": st["sum_min"]},
+                cpu_baseline=cb,
+                e2e={"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
 
 
 def main():
@@ -839,8 +1017,13 @@ def main():
                     help="add U(0,1] vertex weights (seed 4) to a workload that has none")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU leg (reference sample, oracle parity)")
+    ap.add_argument("--no-unweighted", action="store_true",
+                    help="weighted workloads: skip the unweighted calls reported beside")
+    ap.add_argument("--cpu-seconds", type=float, default=20.0,
+                    help="jx arm: seconds of the reference sample behind cpu_baseline")
+    ap.add_argument("--ref-seconds", type=float, default=150.0,
+                    help="reference arm: seconds of reference samples over all timed steps")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "jx":
         log("warm-up raised to 3 steps")

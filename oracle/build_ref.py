@@ -7,8 +7,10 @@ Builds two host libraries with gcc/g++ (no GPU, no cmake):
 * ``oracle/_ref/libjxref.so`` -- the reference's own ``jaccard.cpp`` compiled unmodified
   against the host SYCL subset in ``oracle/syclshim`` (``oracle/ref_driver.cpp`` includes it).
 
-The reference sources are read where they lie (``/root/reference``) or, on a machine without
-that directory, from the git-ignored copy in ``baseline/_ref/src`` that ``--install`` makes.
+The reference sources are read from the directory given by ``--reference-dir`` or the
+environment variable ``JX_REFERENCE_DIR`` (a checkout of vtsynergy/SYCL-Jaccard, read-only),
+else from the git-ignored copy in ``baseline/_ref/src`` that ``--install`` makes from such a
+checkout; that copy is what machines without a checkout build from.
 Only the files the path and its data formats need are used: jaccard.cpp, jaccard.hpp,
 standalone_algorithms.hpp, standalone_csr.hpp, and the CSR/MTX I/O of readMtxToCSR.cpp/.hpp
 and filetypes.cpp/.hpp.
@@ -23,7 +25,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
-REF_DIRS = ["/root/reference", os.path.join(ROOT, "baseline", "_ref", "src")]
+REF_COPY = os.path.join(ROOT, "baseline", "_ref", "src")
 REF_FILES = ["jaccard.cpp", "jaccard.hpp", "standalone_algorithms.hpp", "standalone_csr.hpp",
              "readMtxToCSR.cpp", "readMtxToCSR.hpp", "filetypes.cpp", "filetypes.hpp"]
 ORACLE_SO = os.path.join(HERE, "libjxoracle.so")
@@ -33,21 +35,27 @@ REF_DEFINES = ["-DSTANDALONE", "-DSYCL_1_2_1", "-DDISABLE_DP_WEIGHT", "-DDISABLE
                "-DDISABLE_DP_INDEX"]
 
 
-def ref_source_dir() -> str | None:
-    for d in REF_DIRS:
-        if all(os.path.isfile(os.path.join(d, f)) for f in REF_FILES):
+def _has_sources(d: str | None) -> bool:
+    return bool(d) and all(os.path.isfile(os.path.join(d, f)) for f in REF_FILES)
+
+
+def ref_source_dir(reference_dir: str | None = None) -> str | None:
+    """The first of: reference_dir, $JX_REFERENCE_DIR, baseline/_ref/src that holds the files."""
+    for d in (reference_dir, os.environ.get("JX_REFERENCE_DIR"), REF_COPY):
+        if _has_sources(d):
             return d
     return None
 
 
-def install_copy() -> str:
-    """Copy the hot-path sources of the reference into the git-ignored baseline/_ref/src."""
-    src = REF_DIRS[0]
-    dst = REF_DIRS[1]
-    os.makedirs(dst, exist_ok=True)
+def install_copy(reference_dir: str) -> str:
+    """Copy the hot-path sources of the reference checkout into the git-ignored
+    baseline/_ref/src."""
+    if not _has_sources(reference_dir):
+        raise FileNotFoundError(f"no reference sources ({', '.join(REF_FILES)}) in {reference_dir!r}")
+    os.makedirs(REF_COPY, exist_ok=True)
     for f in REF_FILES:
-        shutil.copy2(os.path.join(src, f), os.path.join(dst, f))
-    return dst
+        shutil.copy2(os.path.join(reference_dir, f), os.path.join(REF_COPY, f))
+    return REF_COPY
 
 
 def _run(cmd: list[str]) -> None:
@@ -70,8 +78,8 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_SO
 
 
-def build_ref(force: bool = False) -> str | None:
-    d = ref_source_dir()
+def build_ref(force: bool = False, reference_dir: str | None = None) -> str | None:
+    d = ref_source_dir(reference_dir)
     if d is None:
         return None
     os.makedirs(os.path.dirname(REF_SO), exist_ok=True)
@@ -88,14 +96,16 @@ def build_ref(force: bool = False) -> str | None:
 
 def main() -> int:
     ap = argparse.ArgumentParser()
+    ap.add_argument("--reference-dir", default=os.environ.get("JX_REFERENCE_DIR"),
+                    help="a checkout of the reference (default: $JX_REFERENCE_DIR)")
     ap.add_argument("--install", action="store_true",
-                    help="copy the reference's hot-path sources into baseline/_ref/src")
+                    help="copy the reference's hot-path sources from --reference-dir into baseline/_ref/src")
     ap.add_argument("--force", action="store_true")
     a = ap.parse_args()
     if a.install:
-        print("copied reference sources to", install_copy())
+        print("copied reference sources to", install_copy(a.reference_dir))
     print("oracle:", build_oracle(a.force))
-    print("reference:", build_ref(a.force) or "unavailable (no reference sources)")
+    print("reference:", build_ref(a.force, a.reference_dir) or "unavailable (no reference sources)")
     return 0
 
 

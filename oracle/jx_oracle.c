@@ -24,7 +24,7 @@
  * oracle reproduces exactly that order, which is also the order of the reference compiled
  * against the host SYCL subset in oracle/syclshim.
  *
- * All entry points are row-parallel with OpenMP; results do not depend on the thread count.
+ * Entry points are row- or edge-parallel with OpenMP; results do not depend on the thread count.
  */
 #include <math.h>
 #include <stdint.h>
@@ -105,6 +105,16 @@ static inline int jxo_found(const int32_t *ind, int32_t left, int32_t right, int
   return 0;
 }
 
+/* Row of stored edge j, r0 <= row < r1 (the last row whose offset is <= j). */
+static inline int32_t jxo_row_of(const int32_t *row_ptr, int32_t r0, int32_t r1, int64_t j) {
+  int32_t lo = r0, hi = r1 - 1;
+  while (lo < hi) {
+    const int32_t mid = lo + (hi - lo + 1) / 2;
+    if ((int64_t)row_ptr[mid] <= j) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
 /*
  * Jaccard_IsKernel (jaccard.cpp:315-400) for rows [r0, r1):
  *   weight_s[j]  = work[row] + work[col]                         (jaccard.cpp:339)
@@ -116,25 +126,25 @@ void jxo_intersect_rows(int32_t r0, int32_t r1, const int32_t *row_ptr, const in
                         const float *w, const float *work, float *weight_i, float *weight_s,
                         int nthreads) {
   jxo_threads(nthreads);
-#pragma omp parallel for schedule(dynamic, 64)
-  for (int32_t row = r0; row < r1; ++row) {
-    for (int32_t j = row_ptr[row]; j < row_ptr[row + 1]; ++j) {
-      const int32_t col = ind[j];
-      const int32_t Ni = row_ptr[row + 1] - row_ptr[row];
-      const int32_t Nj = row_ptr[col + 1] - row_ptr[col];
-      const int32_t ref = (Ni < Nj) ? row : col;
-      const int32_t cur = (Ni < Nj) ? col : row;
-      if (weight_s) weight_s[j] = work[row] + work[col];
-      float acc = weight_i[j];
-      for (int il = 0; il < JXO_IS_I_LANES; ++il) {
-        for (int32_t i = row_ptr[ref] + il; i < row_ptr[ref + 1]; i += JXO_IS_I_LANES) {
-          const int32_t ref_col = ind[i];
-          const float ref_val = w ? w[ref_col] : 1.0f;
-          if (jxo_found(ind, row_ptr[cur], row_ptr[cur + 1] - 1, ref_col)) acc = ref_val + acc;
-        }
+  /* edge-parallel (a hub row spreads over the threads); each edge's sum is sequential */
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t j = row_ptr[r0]; j < (int64_t)row_ptr[r1]; ++j) {
+    const int32_t row = jxo_row_of(row_ptr, r0, r1, j);
+    const int32_t col = ind[j];
+    const int32_t Ni = row_ptr[row + 1] - row_ptr[row];
+    const int32_t Nj = row_ptr[col + 1] - row_ptr[col];
+    const int32_t ref = (Ni < Nj) ? row : col;
+    const int32_t cur = (Ni < Nj) ? col : row;
+    if (weight_s) weight_s[j] = work[row] + work[col];
+    float acc = weight_i[j];
+    for (int il = 0; il < JXO_IS_I_LANES; ++il) {
+      for (int32_t i = row_ptr[ref] + il; i < row_ptr[ref + 1]; i += JXO_IS_I_LANES) {
+        const int32_t ref_col = ind[i];
+        const float ref_val = w ? w[ref_col] : 1.0f;
+        if (jxo_found(ind, row_ptr[cur], row_ptr[cur + 1] - 1, ref_col)) acc = ref_val + acc;
       }
-      weight_i[j] = acc;
     }
+    weight_i[j] = acc;
   }
 }
 
@@ -249,19 +259,19 @@ void jxo_counts_rows(int32_t r0, int32_t r1, const int32_t *row_ptr, const int32
                      int32_t *cnt, int nthreads) {
   jxo_threads(nthreads);
   const int64_t base = row_ptr[r0];
-#pragma omp parallel for schedule(dynamic, 64)
-  for (int32_t row = r0; row < r1; ++row)
-    for (int32_t j = row_ptr[row]; j < row_ptr[row + 1]; ++j) {
-      const int32_t col = ind[j];
-      const int32_t Ni = row_ptr[row + 1] - row_ptr[row];
-      const int32_t Nj = row_ptr[col + 1] - row_ptr[col];
-      const int32_t ref = (Ni < Nj) ? row : col;
-      const int32_t cur = (Ni < Nj) ? col : row;
-      int32_t c = 0;
-      for (int32_t i = row_ptr[ref]; i < row_ptr[ref + 1]; ++i)
-        c += jxo_found(ind, row_ptr[cur], row_ptr[cur + 1] - 1, ind[i]);
-      cnt[j - base] = c;
-    }
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t j = base; j < (int64_t)row_ptr[r1]; ++j) {
+    const int32_t row = jxo_row_of(row_ptr, r0, r1, j);
+    const int32_t col = ind[j];
+    const int32_t Ni = row_ptr[row + 1] - row_ptr[row];
+    const int32_t Nj = row_ptr[col + 1] - row_ptr[col];
+    const int32_t ref = (Ni < Nj) ? row : col;
+    const int32_t cur = (Ni < Nj) ? col : row;
+    int32_t c = 0;
+    for (int32_t i = row_ptr[ref]; i < row_ptr[ref + 1]; ++i)
+      c += jxo_found(ind, row_ptr[cur], row_ptr[cur + 1] - 1, ind[i]);
+    cnt[j - base] = c;
+  }
 }
 
 /*
@@ -283,20 +293,20 @@ void jxo_jaccard_f64_rows(int32_t n, const int32_t *row_ptr, const int32_t *ind,
     S[v] = s;
   }
   const int64_t base = row_ptr[r0];
-#pragma omp parallel for schedule(dynamic, 64)
-  for (int32_t row = r0; row < r1; ++row)
-    for (int32_t j = row_ptr[row]; j < row_ptr[row + 1]; ++j) {
-      const int32_t col = ind[j];
-      const int32_t Ni = row_ptr[row + 1] - row_ptr[row];
-      const int32_t Nj = row_ptr[col + 1] - row_ptr[col];
-      const int32_t ref = (Ni < Nj) ? row : col;
-      const int32_t cur = (Ni < Nj) ? col : row;
-      double I = 0.0;
-      for (int32_t i = row_ptr[ref]; i < row_ptr[ref + 1]; ++i)
-        if (jxo_found(ind, row_ptr[cur], row_ptr[cur + 1] - 1, ind[i]))
-          I += w ? (double)w[ind[i]] : 1.0;
-      out[j - base] = I / (S[row] + S[col] - I);
-    }
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t j = base; j < (int64_t)row_ptr[r1]; ++j) {
+    const int32_t row = jxo_row_of(row_ptr, r0, r1, j);
+    const int32_t col = ind[j];
+    const int32_t Ni = row_ptr[row + 1] - row_ptr[row];
+    const int32_t Nj = row_ptr[col + 1] - row_ptr[col];
+    const int32_t ref = (Ni < Nj) ? row : col;
+    const int32_t cur = (Ni < Nj) ? col : row;
+    double I = 0.0;
+    for (int32_t i = row_ptr[ref]; i < row_ptr[ref + 1]; ++i)
+      if (jxo_found(ind, row_ptr[cur], row_ptr[cur + 1] - 1, ind[i]))
+        I += w ? (double)w[ind[i]] : 1.0;
+    out[j - base] = I / (S[row] + S[col] - I);
+  }
   free(S);
 }
 
@@ -332,4 +342,78 @@ void jxo_jaccard_list(int32_t n, const int32_t *row_ptr, const int32_t *ind, con
     out[p] = acc / (Ws - acc);
   }
   free(S);
+}
+
+/*
+ * Cost proxy of the reference's IS kernel per row (used to extrapolate a timed sample of the
+ * reference's work-groups to the whole call): work[row] = sum over the row's edges of
+ * min(d_u, d_v) * (1 + log2(max(d_u, d_v))), the binary searches of the shorter list
+ * (jaccard.cpp:333-367).
+ */
+void jxo_row_work(int32_t n, const int32_t *row_ptr, const int32_t *ind, double *work, int nthreads) {
+  jxo_threads(nthreads);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int32_t row = 0; row < n; ++row) {
+    const int32_t du = row_ptr[row + 1] - row_ptr[row];
+    double s = 0.0;
+    for (int32_t j = row_ptr[row]; j < row_ptr[row + 1]; ++j) {
+      const int32_t v = ind[j];
+      const int32_t dv = row_ptr[v + 1] - row_ptr[v];
+      const int32_t mn = du < dv ? du : dv, mx = du < dv ? dv : du;
+      s += (double)mn * (1.0 + log2((double)(mx > 1 ? mx : 1)));
+    }
+    work[row] = s;
+  }
+}
+
+/*
+ * Cost proxy per work-group of the reference's dominant kernel, for timing samples that run
+ * every K-th work-group.  Vertex-centric (ec == 0): Jaccard_IsKernel's group g of G =
+ * min(ceil(n / 8), 65535) holds rows 8g .. 8g+7, then every 8G rows further (jaccard.cpp:413-417
+ * and its row grid-stride); edge-centric: Jaccard_ec_unweighted's group g of G =
+ * min(ceil(e / 256), 65535) holds edges 256g .. 256g+255, then every 256G edges further
+ * (jaccard.cpp:750-753).  out[g] = sum over the group's edges of
+ * min(d_u, d_v) * (1 + log2(max(d_u, d_v))).  Returns G.
+ */
+int64_t jxo_group_work(int ec, int32_t n, const int32_t *row_ptr, const int32_t *ind, double *out,
+                       int nthreads) {
+  jxo_threads(nthreads);
+  const int64_t e = row_ptr[n];
+  const int64_t span = ec ? 256 : 8;
+  const int64_t units = ec ? e : n;
+  int64_t G = (units + span - 1) / span;
+  if (G > 65535) G = 65535;
+  if (G < 1) G = 1;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t g = 0; g < G; ++g) {
+    double s = 0.0;
+    for (int64_t base = g * span; base < units; base += span * G)
+      for (int64_t x = base; x < base + span && x < units; ++x) {
+        int64_t j0, j1;
+        int32_t row;
+        if (ec) { /* edge x: its row by binary search */
+          int32_t lo = 0, hi = n - 1;
+          while (lo < hi) {
+            const int32_t mid = lo + (hi - lo + 1) / 2;
+            if ((int64_t)row_ptr[mid] <= x) lo = mid; else hi = mid - 1;
+          }
+          row = lo;
+          j0 = x;
+          j1 = x + 1;
+        } else {
+          row = (int32_t)x;
+          j0 = row_ptr[row];
+          j1 = row_ptr[row + 1];
+        }
+        const int32_t du = row_ptr[row + 1] - row_ptr[row];
+        for (int64_t j = j0; j < j1; ++j) {
+          const int32_t v = ind[j];
+          const int32_t dv = row_ptr[v + 1] - row_ptr[v];
+          const int32_t mn = du < dv ? du : dv, mx = du < dv ? dv : du;
+          s += (double)mn * (1.0 + log2((double)(mx > 1 ? mx : 1)));
+        }
+      }
+    out[g] = s;
+  }
+  return G;
 }

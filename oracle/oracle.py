@@ -49,6 +49,9 @@ def lib():
                                            ctypes.c_int32, _F64, ctypes.c_int]
         L.jxo_jaccard_list.argtypes = [ctypes.c_int32, _I32, _I32, _F32, ctypes.c_int64, _I32, _I32,
                                        _F32, ctypes.c_int]
+        L.jxo_row_work.argtypes = [ctypes.c_int32, _I32, _I32, _F64, ctypes.c_int]
+        L.jxo_group_work.argtypes = [ctypes.c_int, ctypes.c_int32, _I32, _I32, _F64, ctypes.c_int]
+        L.jxo_group_work.restype = ctypes.c_int64
         _oracle = L
     return _oracle
 
@@ -66,6 +69,7 @@ def ref_lib():
         L = ctypes.CDLL(so)
         L.jxref_set_threads.argtypes = [ctypes.c_int]
         L.jxref_set_group_sample.argtypes = [ctypes.c_longlong, ctypes.c_longlong]
+        L.jxref_set_group_mask.argtypes = [ctypes.c_void_p, ctypes.c_longlong]
         L.jxref_jaccard.argtypes = [ctypes.c_int, ctypes.c_int32, ctypes.c_int32, _I32, _I32, _F32,
                                     _F32]
         L.jxref_rowsum.argtypes = [ctypes.c_int32, ctypes.c_int32, _I32, _I32, _F32, _F32]
@@ -123,6 +127,54 @@ def jaccard(row_ptr, col, w=None, edge_centric=False, rows=None, threads=0):
     return out
 
 
+def jaccard_rows_with_sums(row_ptr, col, w, S, rows, threads=0):
+    """Weighted VC oracle for rows [r0, r1) with the row sums S (float32[n]) given, so that
+    several row ranges of one big graph share one row-sum pass."""
+    n = len(row_ptr) - 1
+    r0, r1 = rows
+    out = np.empty(int(row_ptr[r1]) - int(row_ptr[r0]), np.float32)
+    rc = lib().jxo_jaccard_rows(0, n, _p(row_ptr, _I32), _p(col, _I32), _p(w, _F32), r0, r1,
+                                _p(S, _F32), _p(out, _F32), threads)
+    if rc != 0:
+        raise MemoryError("oracle allocation failed")
+    return out
+
+
+def row_work(row_ptr, col, threads=0):
+    """Per-row cost proxy of the reference's IS kernel (float64[n]): sum over the row's edges
+    of min(d_u, d_v) * (1 + log2(max(d_u, d_v)))."""
+    n = len(row_ptr) - 1
+    out = np.empty(n, np.float64)
+    lib().jxo_row_work(n, _p(row_ptr, _I32), _p(col, _I32), _p(out, _F64), threads)
+    return out
+
+
+def group_work(row_ptr, col, edge_centric=False, threads=0):
+    """Cost proxy per work-group of the reference's dominant kernel (Jaccard_IsKernel, or
+    Jaccard_ec_unweighted when edge_centric), float64[G] with G its number of work-groups."""
+    n = len(row_ptr) - 1
+    out = np.empty(65535, np.float64)
+    G = lib().jxo_group_work(1 if edge_centric else 0, n, _p(row_ptr, _I32), _p(col, _I32), _p(out, _F64),
+                             threads)
+    return out[:G].copy()
+
+
+def check_rows(row_ptr, hubs=5, cta_degree=21000, band=2000, tail=3000):
+    """Row ranges that a parity check of a large skewed graph samples: the `hubs` largest rows
+    (ties by id), the row whose degree is closest to `cta_degree`, a band of `band` rows in
+    the middle of the id range and the last `tail` rows.  Returns [(name, r0, r1), ...]."""
+    n = len(row_ptr) - 1
+    d = np.diff(row_ptr.astype(np.int64))
+    out = [(f"hub{k}_deg{int(d[h])}", int(h), int(h) + 1)
+           for k, h in enumerate(np.argsort(-d, kind="stable")[:hubs])]
+    c = int(np.argmin(np.abs(d - cta_degree)))
+    out.append((f"row_deg{int(d[c])}", c, c + 1))
+    m = n // 2
+    out.append(("middle_band", m, min(n, m + band)))
+    out.append(("tail", max(0, n - tail), n))
+    return out
+
+
 def counts(row_ptr, col, rows=None, threads=0):
     n = len(row_ptr) - 1
     r0, r1 = rows if rows is not None else (0, n)
@@ -143,20 +195,25 @@ def jaccard_f64(row_ptr, col, w=None, rows=None, threads=0):
 # ---------------------------------------------------------------- reference (via SYCL subset)
 
 def ref_jaccard(row_ptr, col, w=None, edge_centric=False, threads=0, group_sample=1,
-                group_residue=0):
+                group_residue=0, group_mask=None):
     """Run sygraph::jaccard of the reference; with group_sample=K only work-groups whose id is
-    group_residue modulo K execute (a timing sample: the results are then incomplete)."""
+    group_residue modulo K execute, with group_mask (uint8 array) only the groups g with
+    group_mask[g] != 0 (timing samples: the results are then incomplete)."""
     L = ref_lib()
     if L is None:
         raise RuntimeError("reference sources unavailable")
     L.jxref_set_threads(threads)
     L.jxref_set_group_sample(group_sample, group_residue)
+    if group_mask is not None:
+        group_mask = np.ascontiguousarray(group_mask, np.uint8)
+        L.jxref_set_group_mask(group_mask.ctypes.data, len(group_mask))
     n = len(row_ptr) - 1
     out = np.zeros(len(col), np.float32)
     try:
         L.jxref_jaccard(1 if edge_centric else 0, n, len(col), _p(row_ptr, _I32), _p(col, _I32),
                         _p(w, _F32), _p(out, _F32))
     finally:
+        L.jxref_set_group_mask(None, 0)
         L.jxref_set_group_sample(1, 0)
     return out
 

@@ -65,6 +65,10 @@ void jxref_set_threads(int n) {
  * k = 1 runs everything. */
 void jxref_set_group_sample(long long k, long long residue) { jxshim::set_group_sample(k, residue); }
 
+/* Execute only work-groups g < len with mask[g] != 0 in each launch (timing samples); a NULL
+ * mask restores the stride sample.  The mask must stay valid while calls run. */
+void jxref_set_group_mask(const unsigned char *mask, long long len) { jxshim::set_group_mask(mask, len); }
+
 int jxref_jaccard(int edge_centric, int32_t n, int32_t e, const int32_t *row_ptr,
                   const int32_t *col, const float *vertex_w, float *out) {
   MuteCout mute;

@@ -20,8 +20,9 @@
  *     per-thread arena rebased for each work-group.
  *   - `atomic<uint32_t|uint64_t>` maps onto GCC atomic builtins.
  *
- * Sampling hook (for a bounded CPU baseline): `jxshim::set_group_sample(K)` makes every
- * nd_range launch execute only the work-groups whose linear group id is a multiple of K.
+ * Sampling hooks (for a bounded CPU baseline): `jxshim::set_group_sample(K, r)` makes every
+ * nd_range launch execute only the work-groups whose linear group id g has g % K == r;
+ * `jxshim::set_group_mask(mask, len)` only those with g < len and mask[g] != 0.
  */
 #ifndef JX_SYCLSHIM_SYCL_HPP
 #define JX_SYCLSHIM_SYCL_HPP
@@ -54,9 +55,19 @@ namespace jxshim {
  * stride 1 = run every work-group.  Defined in syclshim.cpp. */
 extern long long g_group_sample;
 extern long long g_group_residue;
+extern const unsigned char *g_group_mask; /* when set, overrides the stride */
+extern long long g_group_mask_len;
 inline void set_group_sample(long long k, long long residue = 0) {
   g_group_sample = k > 0 ? k : 1;
   g_group_residue = residue;
+}
+inline void set_group_mask(const unsigned char *mask, long long len) {
+  g_group_mask = len > 0 ? mask : nullptr;
+  g_group_mask_len = mask ? len : 0;
+}
+inline bool group_selected(long long g) {
+  if (g_group_mask) return g < g_group_mask_len && g_group_mask[g] != 0;
+  return g % g_group_sample == g_group_residue;
 }
 } // namespace jxshim
 
@@ -329,7 +340,6 @@ public:
       total_groups *= ngroups[i];
       items *= r.l.v[i];
     }
-    const long long stride = jxshim::g_group_sample, residue = jxshim::g_group_residue;
     const size_t arena = local_bytes > 0 ? local_bytes : 64;
     auto run_one = [&](size_t glin, bool fibers, char *base) -> bool {
       size_t grp[D];
@@ -360,7 +370,7 @@ public:
     if (total_groups == 0) return;
     /* The first executed group decides whether fibers are needed. */
     long long g0 = 0;
-    while (g0 < (long long)total_groups && g0 % stride != residue) ++g0;
+    while (g0 < (long long)total_groups && !jxshim::group_selected(g0)) ++g0;
     if (g0 >= (long long)total_groups) return;
     std::vector<char> first(arena);
     const bool fibers = run_one((size_t)g0, true, first.data());
@@ -369,7 +379,7 @@ public:
       std::vector<char> local(arena);
 #pragma omp for schedule(dynamic, 1)
       for (long long g = g0 + 1; g < (long long)total_groups; ++g) {
-        if (g % stride != residue) continue;
+        if (!jxshim::group_selected(g)) continue;
         run_one((size_t)g, fibers, local.data());
       }
     }

@@ -20,6 +20,8 @@
 namespace jxshim {
 long long g_group_sample = 1;
 long long g_group_residue = 0;
+const unsigned char *g_group_mask = nullptr;
+long long g_group_mask_len = 0;
 }
 
 namespace cl {

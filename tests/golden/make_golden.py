@@ -3,10 +3,11 @@
 Runs the reference's own ``jaccard.cpp`` (vtsynergy/SYCL-Jaccard), compiled unmodified
 against the host SYCL subset (``oracle/syclshim``, built by ``oracle/build_ref.py``), on
 small synthetic graphs and stores inputs and outputs in ``tests/golden/*.npz``.  Needs the
-reference sources (``/root/reference`` or the ``baseline/_ref/src`` copy); the GPU machine
-only reads the committed ``.npz`` files.
+reference sources: a checkout named by ``JX_REFERENCE_DIR``, or the ``baseline/_ref/src`` copy
+that ``oracle/build_ref.py --install`` makes; the GPU machine only reads the committed
+``.npz`` files.
 
-    python tests/golden/make_golden.py
+    JX_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
