@@ -50,3 +50,14 @@ def test_cpp_header_compiles():
     r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), "-x", "c++", "-"],
                        input=src, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_cpp_dropin_driver_builds_and_links(jx, tmp_path):
+    """The C++ caller of the drop-in header compiles with g++ and links against libjx.so
+    (it runs in the GPU tests)."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests", "dropin"))
+    import driver_build
+    jx.lib()
+    exe = driver_build.build_driver(str(tmp_path), jx._build.LIBJX)
+    assert os.path.exists(exe)

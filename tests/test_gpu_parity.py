@@ -115,6 +115,23 @@ def csr_from_edges(n, edges, symmetric=True):
     return rp, col
 
 
+def with_repeats(rp, col, rows_every, both_ways):
+    """The CSR with the first neighbour of every `rows_every`-th non-empty row listed twice
+    (rows stay sorted); with both_ways the reverse entry is repeated too.  The reference takes
+    such CSRs without validation and counts every stored position."""
+    n = len(rp) - 1
+    adj = [list(col[rp[u]:rp[u + 1]]) for u in range(n)]
+    for u in range(0, n, rows_every):
+        if adj[u]:
+            v = adj[u][0]
+            adj[u].insert(0, v)
+            if both_ways:
+                adj[v].insert(adj[v].index(u), u)
+    out = np.zeros(n + 1, np.int32)
+    out[1:] = np.cumsum([len(a) for a in adj])
+    return out, np.array([x for a in adj for x in a], np.int32)
+
+
 @pytest.mark.parametrize("mode", ["ec", "vc", "vcw"])
 def test_edge_cases(jx, O, mode):
     rng = np.random.default_rng(5)
@@ -128,6 +145,14 @@ def test_edge_cases(jx, O, mode):
         "directed": csr_from_edges(300, [(int(a), int(b)) for a, b in rng.integers(0, 300, (3000, 2)) if a != b],
                                    symmetric=False),
     }
+    # repeated neighbours (each stored position counts, like the reference's binary searches),
+    # on a graph with rows in every degree bin: lane, warp and CTA rows and a hub row
+    hubby = csr_from_edges(30000, [(0, i) for i in range(1, 26000)] + [(1, i) for i in range(2, 600)] +
+                           [(int(a), int(b)) for a, b in rng.integers(2, 30000, (60000, 2)) if a != b])
+    cases["repeats_both_ways"] = with_repeats(*hubby, rows_every=7, both_ways=True)
+    cases["repeats_one_way"] = with_repeats(*hubby, rows_every=5, both_ways=False)
+    cases["repeats_small"] = with_repeats(*csr_from_edges(40, [(i, j) for i in range(40) for j in range(i + 1, 40)]),
+                                          rows_every=3, both_ways=True)
     for name, (rp, col) in cases.items():
         w = jx.graphgen.uniform_weights(len(rp) - 1, seed=7) if mode == "vcw" else None
         want = O.jaccard(rp, col, w, edge_centric=(mode == "ec"))
@@ -145,10 +170,16 @@ def test_empty_graphs(jx):
 
 
 def test_host_entry_point(jx, O):
+    """Host arrays in and out; the device memory kept between calls is reused, released, and
+    the next call after the release maps it again -- same results every time."""
     rp, col = jx.graphgen.rmat(13, 16, seed=41)
     w = jx.graphgen.uniform_weights(len(rp) - 1, seed=42)
-    for ec, ww in ((True, None), (False, None), (False, w)):
-        assert_bitwise(jx.jaccard_host(rp, col, ww, edge_centric=ec), O.jaccard(rp, col, ww, edge_centric=ec))
+    for rep in range(2):
+        for ec, ww in ((True, None), (False, None), (False, w)):
+            assert_bitwise(jx.jaccard_host(rp, col, ww, edge_centric=ec), O.jaccard(rp, col, ww, edge_centric=ec))
+        assert jx.lib().jx_host_release() == 0
+    rp2, col2 = jx.graphgen.rmat(9, 8, seed=43)  # a smaller graph in the same pool
+    assert_bitwise(jx.jaccard_host(rp2, col2), O.jaccard(rp2, col2))
 
 
 def test_csr_check(jx):

@@ -29,6 +29,11 @@ def pool(jx):
     return graphs, uploads
 
 
+def oracle_of(O, g, weighted, ec):
+    rp, col, w = g
+    return O.jaccard(rp, col, w if weighted else None, edge_centric=ec)
+
+
 def alone(jx, g, weighted, ec):
     import torch
     rp, col, w = g
@@ -36,7 +41,7 @@ def alone(jx, g, weighted, ec):
     return jx.jaccard(view, torch.from_numpy(w).cuda() if weighted else None, edge_centric=ec).cpu().numpy()
 
 
-def test_mix_equals_alone(jx, pool):
+def test_mix_equals_alone(jx, O, pool):
     graphs, uploads = pool
     srv = jx.Server(memory_budget=4 << 30, slots=3, fold_edges=200_000, fold_max_edges=2_000_000)
     ids = [srv.add_graph(*g) for g in graphs]
@@ -62,12 +67,15 @@ def test_mix_equals_alone(jx, pool):
     assert st["completed"] == len(reqs) and st["failed"] == 0
     assert st["passes"] < len(reqs) and st["folded_requests"] > 0
     assert st["p99_ms"] >= st["p50_ms"] > 0 and max(lat) <= st["max_ms"] + 1e-6
+    # every request against the oracle on its graph, and against the graph scored alone
     cache = {}
     for (target, g, weighted, ec), out in zip(reqs, outs):
         key = (id(g), weighted, ec)
         if key not in cache:
-            cache[key] = alone(jx, g, weighted, ec)
-        assert np.array_equal(bits(out), bits(cache[key]))
+            cache[key] = (oracle_of(O, g, weighted, ec), alone(jx, g, weighted, ec))
+        want, one = cache[key]
+        assert np.array_equal(bits(out), bits(want)), f"request differs from the oracle (weighted={weighted}, ec={ec})"
+        assert np.array_equal(bits(one), bits(want))
     # the same requests one at a time through the server
     for (target, g, weighted, ec), out in list(zip(reqs, outs))[:12]:
         one = np.empty_like(out)
