@@ -94,10 +94,17 @@ jx_status jx_jaccard_ws(const jx_csr *g, const float *vertex_w, float *out_j, jx
  * Host-buffer form of jx_jaccard: the reference's buffers wrap host memory
  * (main.cpp:196-200), so this entry point takes host arrays, copies them to the device,
  * runs the operator and copies the results back.  Synchronous.  Pinned host memory gives
- * the fastest copies; pageable memory works.
+ * the fastest copies; pageable memory works.  The device buffers come from a memory pool this
+ * library owns (one per device) that keeps freed memory mapped for the next call, on a stream
+ * of the calling thread's own; jx_host_release() returns that memory to the device.
  */
 jx_status jx_jaccard_host(int32_t n, int32_t e, const int32_t *row_ptr, const int32_t *col_idx,
                           const float *vertex_w, float *out_j, jx_algo algo);
+
+/* Waits for the device, then frees the device memory jx_jaccard_host keeps between calls on the
+ * current device.  (The reference frees its temporaries at every call's end,
+ * jaccard.cpp:931-938; keeping them is this library's choice for repeated calls.) */
+jx_status jx_host_release(void);
 
 /*
  * jx_jaccard without any device allocation.  (No counterpart in the reference.)
@@ -109,8 +116,9 @@ jx_status jx_jaccard_host(int32_t n, int32_t e, const int32_t *row_ptr, const in
  * workspace is a fixed array of JX_NOALLOC_SCRATCH_BYTES inside this library (every GPU that
  * loads the library holds it until the process exits), sized for graphs of at most
  * JX_NOALLOC_MAX_VERTICES vertices; larger graphs are rejected with JX_ERR_TOO_LARGE.
- * The first call on a device looks up the array's device address (a host-side set-up step);
- * make that first call before any stream capture.  Every call shares the one array: calls
+ * The first call on a device looks up the array's device address (a host-side set-up step),
+ * and so does the first call after the device's context was reset (cudaDeviceReset); make
+ * those calls before any stream capture.  Every call shares the one array: calls
  * that overlap on the GPU (on different streams, or from different threads) race and must be
  * serialised by the caller.  Asynchronous on `stream`; the work is smaller-grid than
  * jx_jaccard and so slower on large graphs.

@@ -100,6 +100,7 @@ def lib() -> ctypes.CDLL:
             "jx_jaccard_ws": ([ctypes.POINTER(_Csr), _VP, _VP, ctypes.c_int, _VP, ctypes.c_size_t, _VP], ctypes.c_int),
             "jx_jaccard_workspace_size": ([ctypes.POINTER(_Csr), ctypes.c_int, ctypes.c_int], ctypes.c_size_t),
             "jx_jaccard_host": ([i32, i32, _VP, _VP, _VP, _VP, ctypes.c_int], ctypes.c_int),
+            "jx_host_release": ([], ctypes.c_int),
             "jx_jaccard_noalloc": ([ctypes.POINTER(_Csr), _VP, _VP, ctypes.c_int, _VP], ctypes.c_int),
             "jx_rowsum": ([i32, i32, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
             "jx_fill": ([i64, _VP, f32, _VP], ctypes.c_int),

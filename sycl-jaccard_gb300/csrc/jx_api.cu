@@ -98,6 +98,56 @@ __global__ void check_symmetry_kernel(int32_t n, const int32_t *__restrict__ row
   if (__any_sync(kFull, bad) && lane == 0) atomicOr(flags, JX_CSR_ASYMMETRIC);
 }
 
+// ---------------------------------------------------------------- host-buffer entry point state
+// Device memory of jx_jaccard_host comes from a pool this library owns, one per device, whose
+// release threshold keeps freed blocks mapped: calls after the first reuse their device memory
+// instead of mapping gigabytes again (the default pool returns it at every synchronisation).
+// jx_host_release() hands it back.  Each host thread has its own stream per device.
+static std::mutex g_host_mu;
+static std::vector<cudaMemPool_t> g_host_pools;
+
+struct HostStreams {
+  std::vector<cudaStream_t> s;
+  ~HostStreams() {
+    for (cudaStream_t x : s)
+      if (x) cudaStreamDestroy(x);
+  }
+};
+static thread_local HostStreams tl_host_streams;
+
+static jx_status host_stream_and_pool(cudaStream_t *s, cudaMemPool_t *pool) {
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) return set_cuda_error(ce);
+  {
+    std::lock_guard<std::mutex> lock(g_host_mu);
+    if ((int)g_host_pools.size() <= dev) g_host_pools.resize(dev + 1, nullptr);
+    if (!g_host_pools[dev]) {
+      cudaMemPoolProps props = {};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      cudaMemPool_t p = nullptr;
+      if ((ce = cudaMemPoolCreate(&p, &props)) != cudaSuccess) return set_cuda_error(ce);
+      uint64_t keep = UINT64_MAX;
+      if ((ce = cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep)) != cudaSuccess) {
+        cudaMemPoolDestroy(p);
+        return set_cuda_error(ce);
+      }
+      g_host_pools[dev] = p;
+    }
+    *pool = g_host_pools[dev];
+  }
+  auto &v = tl_host_streams.s;
+  if ((int)v.size() <= dev) v.resize(dev + 1, nullptr);
+  if (!v[dev] && (ce = cudaStreamCreateWithFlags(&v[dev], cudaStreamNonBlocking)) != cudaSuccess) {
+    v[dev] = nullptr;
+    return set_cuda_error(ce);
+  }
+  *s = v[dev];
+  return JX_OK;
+}
+
 } // namespace jx
 
 using namespace jx;
@@ -184,18 +234,24 @@ jx_status jx_jaccard_host(int32_t n, int32_t e, const int32_t *row_ptr, const in
   if (n < 0 || e < 0) return JX_ERR_INVALID;
   if (n == 0 || e == 0) return JX_OK;
   if (!row_ptr || !col_idx || !out_j) return JX_ERR_INVALID;
+  if (algo != JX_ALGO_VERTEX_CENTRIC && algo != JX_ALGO_EDGE_CENTRIC) return JX_ERR_INVALID;
   cudaStream_t s = nullptr;
-  cudaError_t ce = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-  if (ce != cudaSuccess) return set_cuda_error(ce);
+  cudaMemPool_t pool = nullptr;
+  jx_status st = host_stream_and_pool(&s, &pool);
+  if (st != JX_OK) return st;
   const bool weighted = vertex_w && algo == JX_ALGO_VERTEX_CENTRIC;
+  const jx_csr shape{n, e, nullptr, nullptr};
+  const size_t ws_bytes = jx_jaccard_workspace_size(&shape, weighted, algo);
   int32_t *d_rp = nullptr, *d_col = nullptr;
   float *d_w = nullptr, *d_out = nullptr;
-  jx_status st = JX_OK;
+  void *d_ws = nullptr;
+  cudaError_t ce;
   do {
-    if ((ce = cudaMallocAsync(&d_rp, sizeof(int32_t) * ((size_t)n + 1), s)) != cudaSuccess ||
-        (ce = cudaMallocAsync(&d_col, sizeof(int32_t) * (size_t)e, s)) != cudaSuccess ||
-        (ce = cudaMallocAsync(&d_out, sizeof(float) * (size_t)e, s)) != cudaSuccess ||
-        (weighted && (ce = cudaMallocAsync(&d_w, sizeof(float) * (size_t)n, s)) != cudaSuccess)) {
+    if ((ce = cudaMallocFromPoolAsync(&d_rp, sizeof(int32_t) * ((size_t)n + 1), pool, s)) != cudaSuccess ||
+        (ce = cudaMallocFromPoolAsync(&d_col, sizeof(int32_t) * (size_t)e, pool, s)) != cudaSuccess ||
+        (ce = cudaMallocFromPoolAsync(&d_out, sizeof(float) * (size_t)e, pool, s)) != cudaSuccess ||
+        (ce = cudaMallocFromPoolAsync(&d_ws, ws_bytes, pool, s)) != cudaSuccess ||
+        (weighted && (ce = cudaMallocFromPoolAsync(&d_w, sizeof(float) * (size_t)n, pool, s)) != cudaSuccess)) {
       st = set_cuda_error(ce);
       break;
     }
@@ -206,20 +262,29 @@ jx_status jx_jaccard_host(int32_t n, int32_t e, const int32_t *row_ptr, const in
       break;
     }
     const jx_csr g{n, e, d_rp, d_col};
-    if ((st = jx_jaccard(&g, weighted ? d_w : nullptr, d_out, algo, (jx_stream_t)s)) != JX_OK) break;
+    if ((st = jx_jaccard_ws(&g, weighted ? d_w : nullptr, d_out, algo, d_ws, ws_bytes, (jx_stream_t)s)) != JX_OK) break;
     if ((ce = cudaMemcpyAsync(out_j, d_out, sizeof(float) * (size_t)e, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
       st = set_cuda_error(ce);
       break;
     }
   } while (0);
-  if (d_rp) cudaFreeAsync(d_rp, s);
-  if (d_col) cudaFreeAsync(d_col, s);
-  if (d_out) cudaFreeAsync(d_out, s);
-  if (d_w) cudaFreeAsync(d_w, s);
+  for (void *p : {(void *)d_rp, (void *)d_col, (void *)d_out, (void *)d_ws, (void *)d_w})
+    if (p) cudaFreeAsync(p, s);
   ce = cudaStreamSynchronize(s);
   if (st == JX_OK && ce != cudaSuccess) st = set_cuda_error(ce);
-  cudaStreamDestroy(s);
   return st;
+}
+
+jx_status jx_host_release(void) {
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) return set_cuda_error(ce);
+  std::lock_guard<std::mutex> lock(g_host_mu);
+  if (dev < (int)g_host_pools.size() && g_host_pools[dev]) {
+    if ((ce = cudaDeviceSynchronize()) != cudaSuccess) return set_cuda_error(ce);
+    if ((ce = cudaMemPoolTrimTo(g_host_pools[dev], 0)) != cudaSuccess) return set_cuda_error(ce);
+  }
+  return JX_OK;
 }
 
 } // extern "C"

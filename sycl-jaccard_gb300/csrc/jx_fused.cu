@@ -33,6 +33,7 @@
 #include "jx_plan.h"
 
 #include <cooperative_groups.h>
+#include <cuda.h>
 
 #include <algorithm>
 #include <mutex>
@@ -1138,9 +1139,11 @@ Plan default_plan() {
 
 // Class-stream capacities no larger than a graph can fill: a class of a task holds at most
 // ceil(d / 8) entries, d the length of the list it walks (<= the maximum degree, <= e), and no row
-// of more than kB2Max tasks means no hub units.  Capacities only size buffers (a class that
-// outgrows its buffer resumes from the adjacency list), so a low hint costs speed, not
-// results.  Capacities stay multiples of 4 (int4 reads of a class).
+// of more than kB2Max tasks means no hub units.  max_degree must be an upper bound of the
+// graph's largest degree (or -1: unknown, e is used): when 8 * cap_b2 covers it, the plan is
+// marked exact and the CTA-row kernel drops its overflow checks, so a hint below the real
+// maximum would let a class write past its stream.  Capacities stay multiples of 4 (int4
+// reads of a class).
 Plan fit_plan(Plan P, int64_t e, int64_t max_degree) {
   const int64_t bound = max_degree >= 0 ? std::min<int64_t>(max_degree, e) : e;
   const int64_t d = std::min<int64_t>(bound, kB2Max);
@@ -1317,23 +1320,61 @@ static Plan noalloc_plan() {
 }
 
 // Device address of g_noalloc_scratch on the current device.  In host code the symbol names a
-// host-side stand-in, not device memory, so the address is looked up once per device (with
-// that device current) and cached.
+// host-side stand-in, not device memory, so the address is looked up with that device current
+// (cudaGetSymbolAddress, which also loads the module on the device's first use) and cached per
+// device together with the id of the context it belongs to.  A device reset destroys that
+// context and the module with it; the next call sees a new context id and looks the address
+// up again instead of using a stale one.  The driver's context calls are reached through the
+// runtime's entry-point query, so the library needs no link to the driver library.
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+
+static jx_status current_context_id(unsigned long long *id) {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult q;
+    void *f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  });
+  CUcontext ctx = nullptr;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, id) != CUDA_SUCCESS)
+    return JX_ERR_CUDA;
+  return JX_OK;
+}
+
 static jx_status noalloc_scratch(char **ptr) {
+  struct Entry {
+    unsigned long long ctx_id = 0;
+    void *addr = nullptr;
+  };
   static std::mutex mu;
-  static std::vector<void *> addr;
+  static std::vector<Entry> cache;
   int dev = 0;
   cudaError_t ce = cudaGetDevice(&dev);
   if (ce != cudaSuccess) return set_cuda_error(ce);
+  // makes the device's primary context current (and creates it after a reset); allocates nothing
+  if ((ce = cudaSetDevice(dev)) != cudaSuccess) return set_cuda_error(ce);
+  unsigned long long id = 0;
+  if (current_context_id(&id) != JX_OK) return JX_ERR_CUDA;
   std::lock_guard<std::mutex> lock(mu);
-  if ((int)addr.size() <= dev) addr.resize(dev + 1, nullptr);
-  if (!addr[dev]) {
+  if ((int)cache.size() <= dev) cache.resize(dev + 1);
+  Entry &en = cache[dev];
+  if (!en.addr || en.ctx_id != id) {
     void *p = nullptr;
     ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (ce != cudaSuccess) return set_cuda_error(ce);
-    addr[dev] = p;
+    en.addr = p;
+    en.ctx_id = id;
   }
-  *ptr = static_cast<char *>(addr[dev]);
+  *ptr = static_cast<char *>(en.addr);
   return JX_OK;
 }
 

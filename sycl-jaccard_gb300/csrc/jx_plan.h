@@ -23,7 +23,8 @@ struct Plan {
 
 Plan default_plan();
 // P with its class-stream capacities cut to what a graph of e edges and the given maximum
-// degree (-1: unknown) can use; results do not depend on the capacities.
+// degree can use.  max_degree must be an upper bound of the graph's largest degree (-1:
+// unknown); results do not depend on the capacities as long as it is.
 Plan fit_plan(Plan P, int64_t e, int64_t max_degree);
 // Workspace bytes of one call under plan P.
 size_t plan_workspace(int32_t n, int32_t e, bool weighted_vc, const Plan &P);
