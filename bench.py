@@ -189,10 +189,10 @@ def max_over_ranks(x, world):
     return float(t.item())
 
 
-def make_graph(name, threads):
+def make_graph(name, threads, permute=0):
     jx = importlib.import_module("sycl-jaccard_gb300")
     t = time.time()
-    rp, col, w, desc = jx.graphgen.config_graph(name, threads=threads)
+    rp, col, w, desc = jx.graphgen.config_graph(name, threads=threads, permute=permute)
     st = jx.graphgen.stats(rp, col)
     log(f"graph {name}: V={st['V']} E={st['E']} max_deg={st['max_degree']} sum_min={st['sum_min']:.4g} "
         f"({time.time() - t:.1f}s)")
@@ -827,7 +827,7 @@ def run_gpu(args, world, rank, local):
     jx = importlib.import_module("sycl-jaccard_gb300")
     torch.cuda.set_device(local)
     threads = os.cpu_count() or 1
-    rp, col, w, desc, st = make_graph(args.workload, threads)
+    rp, col, w, desc, st = make_graph(args.workload, threads, args.permute)
     if args.unweighted:
         w, desc = None, desc + " (weights dropped: unweighted)"
     elif args.weighted and w is None:
@@ -975,7 +975,7 @@ def run_reference(args, world, rank):
         return dict(common, value=value, ms_per_step=round(bs.E / value * 1e3, 3), config=config,
                     cpu_baseline=cb,
                     e2e={"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
-    rp, col, w, desc, st = make_graph(args.workload, threads)
+    rp, col, w, desc, st = make_graph(args.workload, threads, args.permute)
     weighted = w is not None and not args.ec
     sm = RefSampler(rp, col, w if weighted else None, edge_centric=args.ec, threads=threads)
     if args.warmup > 0:
@@ -1012,6 +1012,8 @@ def main():
     ap.add_argument("--light-requests", type=int, default=300,
                     help="served: requests of the second trace at half the sustained rate (0: skip)")
     ap.add_argument("--ec", action="store_true", help="edge-centric algorithm")
+    ap.add_argument("--permute", type=int, default=0,
+                    help="R-MAT workloads: relabel the vertex ids by a bijection with this seed (0: none)")
     ap.add_argument("--unweighted", action="store_true", help="drop the vertex weights")
     ap.add_argument("--weighted", action="store_true",
                     help="add U(0,1] vertex weights (seed 4) to a workload that has none")

@@ -107,10 +107,12 @@ extern "C" {
 /*
  * R-MAT graph: 2^scale vertices, edge_factor * 2^scale undirected samples with quadrant
  * probabilities (a, b, c, 1-a-b-c), then symmetrised / deduplicated / loop-free.
- * No vertex relabelling is applied: high-degree vertices keep small ids.
+ * With perm_seed == 0 no vertex relabelling is applied (high-degree vertices keep small ids);
+ * otherwise every id v becomes jx_permute_bits(v, scale, perm_seed), a seeded bijection, so
+ * the graph is the same up to the names of its vertices.
  */
 void *jxg_rmat(int scale, int64_t edge_factor, double a, double b, double c, uint64_t seed,
-               int nthreads) {
+               uint64_t perm_seed, int nthreads) {
   if (scale < 1 || scale > 30 || edge_factor < 1) return nullptr;
   set_threads(nthreads);
   const int64_t n = (int64_t)1 << scale;
@@ -119,7 +121,13 @@ void *jxg_rmat(int scale, int64_t edge_factor, double a, double b, double c, uin
   try {
     std::vector<uint32_t> src(m), dst(m);
 #pragma omp parallel for schedule(static)
-    for (int64_t i = 0; i < m; ++i) jx_rmat_sample(seed, (uint64_t)i, scale, t0, t1, t2, &src[i], &dst[i]);
+    for (int64_t i = 0; i < m; ++i) {
+      jx_rmat_sample(seed, (uint64_t)i, scale, t0, t1, t2, &src[i], &dst[i]);
+      if (perm_seed) {
+        src[i] = jx_permute_bits(src[i], scale, perm_seed);
+        dst[i] = jx_permute_bits(dst[i], scale, perm_seed);
+      }
+    }
     return build_symmetric(n, src, dst);
   } catch (const std::bad_alloc &) {
     return nullptr;

@@ -70,4 +70,21 @@ JX_HD void jx_rmat_sample(uint64_t seed, uint64_t sample, int scale, uint32_t t0
   *dst = c;
 }
 
+/*
+ * A seeded bijection of [0, 2^bits) (1 <= bits <= 32) for relabelling vertex ids: four rounds
+ * of (multiply by an odd key, xor with the upper half shifted down, add a key), each step a
+ * bijection modulo 2^bits.
+ */
+JX_HD uint32_t jx_permute_bits(uint32_t x, int bits, uint64_t seed) {
+  const uint32_t mask = bits >= 32 ? 0xFFFFFFFFu : ((1u << bits) - 1u);
+  const int shift = (bits + 1) / 2;
+  for (uint64_t r = 0; r < 4; ++r) {
+    const uint64_t k = jx_draw(seed, 0x5045524Dull, r);
+    x = (x * ((uint32_t)k | 1u)) & mask;
+    x ^= x >> shift;
+    x = (x + (uint32_t)(k >> 32)) & mask;
+  }
+  return x;
+}
+
 #endif /* JX_RNG_H */

@@ -25,7 +25,7 @@ def _lib():
         L = ctypes.CDLL(_build.LIBGEN)
         L.jxg_rmat.restype = ctypes.c_void_p
         L.jxg_rmat.argtypes = [ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_double,
-                               ctypes.c_double, ctypes.c_uint64, ctypes.c_int]
+                               ctypes.c_double, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int]
         L.jxg_er_gnp.restype = ctypes.c_void_p
         L.jxg_er_gnp.argtypes = [ctypes.c_int64, ctypes.c_double, ctypes.c_uint64, ctypes.c_int]
         L.jxg_er_gnm.restype = ctypes.c_void_p
@@ -57,9 +57,11 @@ def _take(h):
 
 
 def rmat(scale: int, edge_factor: int = 16, a: float = 0.57, b: float = 0.19, c: float = 0.19,
-         seed: int = 0, threads: int = 0):
-    """R-MAT(scale, edge_factor, a, b, c), symmetrised / deduplicated / loop-free int32 CSR."""
-    return _take(_lib().jxg_rmat(scale, edge_factor, a, b, c, seed, threads))
+         seed: int = 0, threads: int = 0, permute: int = 0):
+    """R-MAT(scale, edge_factor, a, b, c), symmetrised / deduplicated / loop-free int32 CSR.
+    permute != 0 relabels the vertices by a bijection of [0, 2^scale) seeded by it (the same
+    graph with hub ids scattered over the id range)."""
+    return _take(_lib().jxg_rmat(scale, edge_factor, a, b, c, seed, permute, threads))
 
 
 def er_gnp(n: int, p: float, seed: int = 0, threads: int = 0):
@@ -95,20 +97,28 @@ def stats(row_ptr: np.ndarray, col: np.ndarray) -> dict:
 
 
 # Named configurations (the benchmark's workload shapes).
-def config_graph(name: str, threads: int = 0):
-    """Returns (row_ptr, col_idx, vertex_weights or None, description)."""
+def config_graph(name: str, threads: int = 0, permute: int = 0):
+    """Returns (row_ptr, col_idx, vertex_weights or None, description).  permute != 0 relabels
+    the vertices of the R-MAT configurations (see rmat)."""
+    if permute and name.startswith("rmat"):
+        rp, col, w, desc = _config_graph(name, threads, permute)
+        return rp, col, w, desc + f", vertex ids relabelled by a bijection seeded {permute}"
+    return _config_graph(name, threads, 0)
+
+
+def _config_graph(name: str, threads: int, permute: int):
     if name == "er4096":
         rp, col = er_gnp(4096, 16.0 / 4095.0, seed=1, threads=threads)
         return rp, col, np.ones(4096, np.float32), "ER G(4096, 16/4095) seed 1, unit weights"
     if name == "rmat20":
-        rp, col = rmat(20, 16, 0.57, 0.19, 0.19, seed=2, threads=threads)
+        rp, col = rmat(20, 16, 0.57, 0.19, 0.19, seed=2, threads=threads, permute=permute)
         return rp, col, None, "RMAT scale 20 ef 16 (.57,.19,.19,.05) seed 2, unweighted"
     if name == "rmat22w":  # the headline shape at a quarter of the size (profiling captures)
-        rp, col = rmat(22, 16, 0.57, 0.19, 0.19, seed=3, threads=threads)
+        rp, col = rmat(22, 16, 0.57, 0.19, 0.19, seed=3, threads=threads, permute=permute)
         w = uniform_weights(len(rp) - 1, seed=4, threads=threads)
         return rp, col, w, "RMAT scale 22 ef 16 (.57,.19,.19,.05) seed 3, vertex weights U(0,1] seed 4"
     if name == "rmat24w":
-        rp, col = rmat(24, 16, 0.57, 0.19, 0.19, seed=3, threads=threads)
+        rp, col = rmat(24, 16, 0.57, 0.19, 0.19, seed=3, threads=threads, permute=permute)
         w = uniform_weights(len(rp) - 1, seed=4, threads=threads)
         return rp, col, w, "RMAT scale 24 ef 16 (.57,.19,.19,.05) seed 3, vertex weights U(0,1] seed 4"
     raise KeyError(name)

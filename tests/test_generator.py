@@ -47,3 +47,18 @@ def test_stats(jx):
     src = np.repeat(np.arange(len(d)), d)
     assert st["sum_min"] == int(np.minimum(d[src], d[col]).sum())
     assert st["V"] == 1024 and st["E"] == len(col)
+
+
+def test_rmat_permuted_is_the_same_graph_relabelled(jx, O):
+    """A relabelled R-MAT has the same degree sequence and, edge for edge, the same Jaccard
+    values as a multiset; its hub no longer sits at vertex 0."""
+    rp, col = jx.graphgen.rmat(11, 16, seed=9)
+    rq, cq = jx.graphgen.rmat(11, 16, seed=9, permute=77)
+    assert len(cq) == len(col) and len(rq) == len(rp)
+    d, dq = np.diff(rp), np.diff(rq)
+    assert np.array_equal(np.sort(d), np.sort(dq))
+    assert int(np.argmax(dq)) != int(np.argmax(d))
+    check_csr(rq, cq)
+    J, Jq = O.jaccard(rp, col), O.jaccard(rq, cq)
+    assert np.array_equal(np.sort(J.view(np.uint32)), np.sort(Jq.view(np.uint32)))
+    assert not np.array_equal(rp, rq)
