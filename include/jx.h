@@ -39,7 +39,8 @@ typedef enum {
   JX_ERR_NOMEM = 3,       /* device or host allocation failed */
   JX_ERR_BAD_GRAPH = 4,   /* jx_csr_check found an invalid CSR */
   JX_ERR_UNSUPPORTED = 5, /* valid request outside what this library supports */
-  JX_ERR_TOO_LARGE = 6    /* size above a documented maximum */
+  JX_ERR_TOO_LARGE = 6,   /* size above a documented maximum */
+  JX_ERR_CANCELLED = 7    /* a server request was cancelled before it started */
 } jx_status;
 
 typedef enum {
@@ -279,6 +280,7 @@ typedef struct {
   double p50_ms, p99_ms, mean_ms, max_ms; /* arrival -> results in host memory */
   double span_s;            /* first arrival -> last completion */
   size_t peak_reserved;     /* most device bytes admitted at once (resident graphs included) */
+  uint64_t cancelled;       /* requests cancelled before they started (not in `failed`) */
 } jx_server_stats;
 
 typedef struct jx_server_s *jx_server;
@@ -297,6 +299,19 @@ jx_status jx_server_get_stats(jx_server s, jx_server_stats *out);
 void jx_server_reset_stats(jx_server s);
 /* The server's clock (monotonic, nanoseconds) for jx_request.arrival_ns. */
 int64_t jx_server_clock_ns(void);
+/* paused != 0: admit nothing new (passes already started run to completion; submitted requests
+ * wait in the queue); paused == 0: resume admission. */
+jx_status jx_server_set_paused(jx_server s, int32_t paused);
+/* Cancel a request that has not started: JX_OK, its jx_server_wait returns JX_ERR_CANCELLED and
+ * its host buffer is not written.  JX_ERR_UNSUPPORTED when it has already started or finished
+ * (it runs to completion); JX_ERR_INVALID for an unknown ticket.  (The reference reports a
+ * failed kernel and carries on, jaccard.cpp:178-180; a request here fails alone likewise.) */
+jx_status jx_server_cancel(jx_server s, uint64_t ticket);
+/* Failure injection for tests of the server's error handling, on the host: the next `count`
+ * device allocations made for passes fail as if the device were out of memory, without calling
+ * the allocator.  The requests of an affected pass complete with JX_ERR_NOMEM; other passes
+ * and requests are unaffected. */
+jx_status jx_server_inject_alloc_failures(jx_server s, int32_t count);
 /* Drains, then releases every resident graph and the server's threads and streams. */
 void jx_server_destroy(jx_server s);
 

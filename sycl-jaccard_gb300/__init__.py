@@ -35,7 +35,8 @@ __all__ = ["GraphCSRView", "JxError", "jaccard", "jaccard_host", "jaccard_noallo
 
 JX_OK = 0
 _STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory",
-           4: "invalid CSR graph", 5: "unsupported request", 6: "size above the supported maximum"}
+           4: "invalid CSR graph", 5: "unsupported request", 6: "size above the supported maximum",
+           7: "request cancelled"}
 ALGO_VERTEX_CENTRIC = 0
 ALGO_EDGE_CENTRIC = 1
 
@@ -71,7 +72,8 @@ class _ServerStats(ctypes.Structure):
     _fields_ = [("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64), ("passes", ctypes.c_uint64),
                 ("folded_requests", ctypes.c_uint64), ("kernels", ctypes.c_uint64), ("edges", ctypes.c_int64),
                 ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
-                ("max_ms", ctypes.c_double), ("span_s", ctypes.c_double), ("peak_reserved", ctypes.c_size_t)]
+                ("max_ms", ctypes.c_double), ("span_s", ctypes.c_double), ("peak_reserved", ctypes.c_size_t),
+                ("cancelled", ctypes.c_uint64)]
 
 
 class _Csr(ctypes.Structure):
@@ -132,6 +134,9 @@ def lib() -> ctypes.CDLL:
             "jx_server_reset_stats": ([_VP], None),
             "jx_server_clock_ns": ([], ctypes.c_int64),
             "jx_server_destroy": ([_VP], None),
+            "jx_server_set_paused": ([_VP, i32], ctypes.c_int),
+            "jx_server_cancel": ([_VP, ctypes.c_uint64], ctypes.c_int),
+            "jx_server_inject_alloc_failures": ([_VP, i32], ctypes.c_int),
             "jx_status_string": ([ctypes.c_int], ctypes.c_char_p),
             "jx_version": ([], ctypes.c_int),
             "jx_last_cuda_error": ([], ctypes.c_int),
@@ -514,6 +519,23 @@ class Server:
 
     def drain(self):
         _check(lib().jx_server_drain(self._h), "jx_server_drain")
+
+    def pause(self, paused: bool = True):
+        """Hold (or, with False, resume) admission; passes already started run on."""
+        _check(lib().jx_server_set_paused(self._h, int(paused)), "jx_server_set_paused")
+
+    def cancel(self, ticket: int) -> bool:
+        """Cancel a request that has not started: True if cancelled (its wait raises JxError
+        with status 7), False if it had already started or finished."""
+        st = lib().jx_server_cancel(self._h, ticket)
+        if st == 5:
+            return False
+        _check(st, "jx_server_cancel")
+        return True
+
+    def inject_alloc_failures(self, count: int):
+        """Test hook: the next `count` device allocations of passes fail as out of memory."""
+        _check(lib().jx_server_inject_alloc_failures(self._h, count), "jx_server_inject_alloc_failures")
 
     def stats(self) -> dict:
         st = _ServerStats()

@@ -163,6 +163,7 @@ const char *jx_status_string(jx_status s) {
   case JX_ERR_BAD_GRAPH: return "invalid CSR graph";
   case JX_ERR_UNSUPPORTED: return "unsupported request";
   case JX_ERR_TOO_LARGE: return "size above the supported maximum";
+  case JX_ERR_CANCELLED: return "request cancelled";
   }
   return "unknown status";
 }

@@ -83,6 +83,8 @@ struct jx_server_s {
   size_t reserved = 0, peak_reserved = 0, resident_bytes = 0;
   std::vector<Resident> graphs;
   bool stop = false;
+  bool paused = false;                  // admission held (jx_server_set_paused)
+  std::atomic<int32_t> inject_alloc{0}; // allocations still to fail (jx_server_inject_alloc_failures)
 
   // slots
   struct Slot {
@@ -98,7 +100,7 @@ struct jx_server_s {
 
   // statistics (guarded by mu)
   std::vector<double> lat_ms;
-  uint64_t completed = 0, failed = 0, passes = 0, folded = 0;
+  uint64_t completed = 0, failed = 0, cancelled = 0, passes = 0, folded = 0;
   int64_t edges = 0;
   int64_t first_arrival = 0, last_done = 0;
   std::atomic<uint64_t> kernels{0};
@@ -145,14 +147,27 @@ size_t fold_bytes(const std::vector<Req *> &reqs) {
 bool foldable(const jx_server_s *S, const Req *r) { return r->e <= S->cfg.fold_edges; }
 bool same_kind(const Req *a, const Req *b) { return a->algo == b->algo && a->weighted == b->weighted; }
 
+// Take one injected allocation failure, if any are left.
+bool take_injected(std::atomic<int32_t> *left) {
+  int32_t v = left ? left->load() : 0;
+  while (v > 0 && !left->compare_exchange_weak(v, v - 1)) {
+  }
+  return v > 0;
+}
+
 struct DevBuf {
   cudaMemPool_t pool;
   cudaStream_t s;
+  std::atomic<int32_t> *inject = nullptr;
   std::vector<void *> ptrs;
   cudaError_t err = cudaSuccess;
   template <class T> T *get(size_t count) {
     void *p = nullptr;
     if (err != cudaSuccess) return nullptr;
+    if (take_injected(inject)) {
+      err = cudaErrorMemoryAllocation;
+      return nullptr;
+    }
     err = cudaMallocFromPoolAsync(&p, std::max<size_t>(align_up(sizeof(T) * count), 256), pool, s);
     if (err != cudaSuccess) return nullptr;
     ptrs.push_back(p);
@@ -172,7 +187,7 @@ struct DevBuf {
 // One request on its own graph.
 jx_status run_single(jx_server_s *S, Req &r, cudaStream_t s) {
   if (r.e == 0) return JX_OK;
-  DevBuf buf{S->pool, s};
+  DevBuf buf{S->pool, s, &S->inject_alloc};
   const Plan P = fit_plan(default_plan(), r.e, r.max_deg);
   jx_csr g{r.n, r.e, nullptr, nullptr};
   const float *w = nullptr, *row_sums = nullptr;
@@ -219,7 +234,7 @@ jx_status run_fold(jx_server_s *S, std::vector<Req *> &reqs, cudaStream_t s) {
   const bool weighted = reqs[0]->weighted;
   const jx_algo algo = reqs[0]->algo;
   const Plan P = fold_plan(reqs, ne);
-  DevBuf buf{S->pool, s};
+  DevBuf buf{S->pool, s, &S->inject_alloc};
   int32_t *rp = buf.get<int32_t>((size_t)nv + 1);
   int32_t *col = buf.get<int32_t>((size_t)ne);
   float *w = weighted ? buf.get<float>((size_t)nv) : nullptr;
@@ -310,9 +325,9 @@ void dispatcher_main(jx_server_s *S) {
   cudaSetDevice(S->device);
   std::unique_lock<std::mutex> lock(S->mu);
   for (;;) {
-    S->cv_queue.wait(lock, [&] { return S->stop || (!S->queue.empty() && S->free_slots > 0); });
+    S->cv_queue.wait(lock, [&] { return S->stop || (!S->paused && !S->queue.empty() && S->free_slots > 0); });
     if (S->queue.empty() && S->stop) return;
-    if (S->queue.empty() || S->free_slots == 0) continue;
+    if (S->queue.empty() || S->free_slots == 0 || (S->paused && !S->stop)) continue;
     Req *head = S->queue.front();
     const size_t budget = S->cfg.memory_budget;
     if (S->resident_bytes + head->need > budget) { // can never fit
@@ -326,7 +341,11 @@ void dispatcher_main(jx_server_s *S) {
       continue;
     }
     if (S->resident_bytes + S->reserved + head->need > budget) { // wait for memory, in arrival order
-      S->cv_queue.wait(lock, [&] { return S->stop || S->resident_bytes + S->reserved + head->need <= budget; });
+      // (or for the head to be cancelled: the queue front then changes)
+      S->cv_queue.wait(lock, [&] {
+        return S->stop || S->queue.empty() || S->queue.front() != head ||
+               S->resident_bytes + S->reserved + head->need <= budget;
+      });
       continue;
     }
     auto pass = std::make_unique<Pass>();
@@ -520,6 +539,39 @@ jx_status jx_server_wait(jx_server S, uint64_t ticket, double *latency_ms) {
   return st;
 }
 
+jx_status jx_server_set_paused(jx_server S, int32_t paused) {
+  if (!S) return JX_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(S->mu);
+  S->paused = paused != 0;
+  S->cv_queue.notify_all();
+  return JX_OK;
+}
+
+jx_status jx_server_cancel(jx_server S, uint64_t ticket) {
+  if (!S) return JX_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(S->mu);
+  auto it = S->reqs.find(ticket);
+  if (it == S->reqs.end()) return JX_ERR_INVALID;
+  Req *r = it->second.get();
+  auto q = std::find(S->queue.begin(), S->queue.end(), r);
+  if (r->done || q == S->queue.end()) return JX_ERR_UNSUPPORTED; // started or finished
+  S->queue.erase(q);
+  r->status = JX_ERR_CANCELLED;
+  r->done_ns = now_ns();
+  r->done = true;
+  ++S->cancelled;
+  ++S->finished;
+  S->cv_queue.notify_all();
+  S->cv_done.notify_all();
+  return JX_OK;
+}
+
+jx_status jx_server_inject_alloc_failures(jx_server S, int32_t count) {
+  if (!S || count < 0) return JX_ERR_INVALID;
+  S->inject_alloc.store(count);
+  return JX_OK;
+}
+
 jx_status jx_server_drain(jx_server S) {
   if (!S) return JX_ERR_INVALID;
   std::unique_lock<std::mutex> lock(S->mu);
@@ -533,6 +585,7 @@ jx_status jx_server_get_stats(jx_server S, jx_server_stats *o) {
   *o = jx_server_stats{};
   o->completed = S->completed;
   o->failed = S->failed;
+  o->cancelled = S->cancelled;
   o->passes = S->passes;
   o->folded_requests = S->folded;
   o->kernels = S->kernels.load();
@@ -560,7 +613,7 @@ void jx_server_reset_stats(jx_server S) {
   if (!S) return;
   std::lock_guard<std::mutex> lock(S->mu);
   S->lat_ms.clear();
-  S->completed = S->failed = S->passes = S->folded = 0;
+  S->completed = S->failed = S->cancelled = S->passes = S->folded = 0;
   S->edges = 0;
   S->first_arrival = S->last_done = 0;
   S->peak_reserved = S->resident_bytes + S->reserved;
@@ -569,6 +622,7 @@ void jx_server_reset_stats(jx_server S) {
 
 void jx_server_destroy(jx_server S) {
   if (!S) return;
+  jx_server_set_paused(S, 0); // queued requests run before the server goes away
   jx_server_drain(S);
   {
     std::lock_guard<std::mutex> lock(S->mu);

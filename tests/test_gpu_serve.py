@@ -103,3 +103,65 @@ def test_admission_budget(jx, pool):
     with pytest.raises(jx.JxError):
         srv.submit(gid, np.empty(len(small[1]), np.float32), weighted=True)
     srv.close()
+
+
+def test_injected_alloc_failure_fails_one_pass_only(jx, O, pool):
+    """An allocation failure inside one pass (injected on the host) fails that pass's request
+    with JX_ERR_NOMEM; every other request completes bit for bit, and the failed one succeeds
+    when submitted again."""
+    graphs, _ = pool
+    srv = jx.Server(memory_budget=2 << 30, slots=2, fold_edges=0)  # no folding: a pass per request
+    ids = [srv.add_graph(*g) for g in graphs[:4]]
+    srv.pause()
+    outs = [np.empty(len(g[1]), np.float32) for g in graphs[:4]]
+    tickets = [srv.submit(gid, out, weighted=True) for gid, out in zip(ids, outs)]
+    srv.inject_alloc_failures(1)
+    srv.pause(False)
+    failed = []
+    for k, t in enumerate(tickets):
+        try:
+            srv.wait(t)
+        except jx.JxError as e:
+            assert e.status == 3  # JX_ERR_NOMEM
+            failed.append(k)
+    assert len(failed) == 1
+    for k, (rp, col, w) in enumerate(graphs[:4]):
+        if k not in failed:
+            assert np.array_equal(bits(outs[k]), bits(O.jaccard(rp, col, w)))
+    k = failed[0]
+    again = np.empty_like(outs[k])
+    srv.wait(srv.submit(ids[k], again, weighted=True))
+    assert np.array_equal(bits(again), bits(O.jaccard(*graphs[k])))
+    st = srv.stats()
+    assert st["failed"] == 1 and st["completed"] == 4
+    srv.close()
+
+
+def test_cancel_queued_request(jx, O, pool):
+    """A request cancelled while it waits in the queue never runs: its wait reports
+    JX_ERR_CANCELLED and its host buffer is untouched; the requests around it complete bit for
+    bit.  Requests that have finished can no longer be cancelled."""
+    graphs, uploads = pool
+    srv = jx.Server(memory_budget=2 << 30, slots=1)
+    srv.pause()
+    reqs = [graphs[0], uploads[1], graphs[2]]
+    outs = [np.full(len(g[1]), np.nan, np.float32) for g in reqs]
+    tickets = [srv.submit(g, out, weighted=True) for g, out in zip(reqs, outs)]
+    assert srv.cancel(tickets[1]) is True
+    srv.pause(False)
+    for k in (0, 2):
+        srv.wait(tickets[k])
+        assert np.array_equal(bits(outs[k]), bits(O.jaccard(*reqs[k])))
+    with pytest.raises(jx.JxError) as e:
+        srv.wait(tickets[1])
+    assert e.value.status == 7
+    assert np.all(np.isnan(outs[1]))
+    t = srv.submit(uploads[0], np.empty(len(uploads[0][1]), np.float32), weighted=True)
+    srv.drain()
+    assert srv.cancel(t) is False  # finished: nothing to cancel
+    srv.wait(t)
+    with pytest.raises(jx.JxError):
+        srv.cancel(t)  # unknown after its wait
+    st = srv.stats()
+    assert st["cancelled"] == 1 and st["failed"] == 0 and st["completed"] == 3
+    srv.close()
