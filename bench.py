@@ -682,23 +682,23 @@ def run_gpu_served(args, world, rank, local):
         alone[key] = np.empty(edges[key], np.float32)
         plain(key, alone[key])
 
-    # serial plain launches over the same request sequence, back to back
+    # the serial plain server, run for real: the same trace replayed at its arrival times, one
+    # request at a time in arrival order (a request starts when it has arrived and the one
+    # before it is done); latency = arrival -> results in host memory
     torch.cuda.synchronize()
-    svc = []
     scratch = {}
-    tp0 = time.perf_counter()
-    for key in trace_g:
-        a = time.perf_counter()
+    plat = []
+    tp0 = time.perf_counter() + 0.002
+    for at, key in zip(trace_t, trace_g):
+        due = tp0 + float(at)
+        now = time.perf_counter()
+        if now < due:
+            time.sleep(due - now)
         out = scratch.setdefault(key, np.empty(edges[key], np.float32))
         plain(key, out)
-        svc.append(time.perf_counter() - a)
-    plain_s = time.perf_counter() - tp0
+        plat.append((time.perf_counter() - due) * 1e3)
+    plain_s = time.perf_counter() - tp0 - float(trace_t[0])
     E_trace = sum(edges[k] for k in trace_g)
-    # the serial server's latencies under the same arrivals (queue of one, measured service times)
-    fin, plat = 0.0, []
-    for at, sv in zip(trace_t, svc):
-        fin = max(fin, at) + sv
-        plat.append((fin - at) * 1e3)
     plat.sort()
 
     # warm-up requests, then the timed replay
@@ -755,9 +755,8 @@ def run_gpu_served(args, world, rank, local):
         "plain": {"value": E_trace / plain_s, "unit": UNIT, "seconds": round(plain_s, 4),
                   "p50_ms": round(plat[len(plat) // 2], 3),
                   "p99_ms": round(plat[min(len(plat) - 1, int(np.ceil(0.99 * len(plat))) - 1)], 3),
-                  "what": "the same requests one at a time: jx_jaccard + copy-out (resident), "
-                          "jx_jaccard_host (uploads); latencies of a one-at-a-time server under the "
-                          "same arrivals from the measured service times"},
+                  "what": "the same trace replayed at its arrival times through a one-at-a-time server: "
+                          "jx_jaccard + copy-out (resident), jx_jaccard_host (uploads); measured latencies"},
         "served_over_plain": round(value / (E_trace / plain_s), 3),
         "served_light_load": light,
         "clocks": clocks,
@@ -884,6 +883,17 @@ def run_gpu(args, world, rank, local):
         e2e = {"value": E * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": 4 * E, "ms_per_step": round(e2e_s * 1e3, 3),
                "timing": "host wall clock around the synchronous call"}
+        # where one host call's time goes: stream events after its copies in, each kernel and
+        # its copy out (event gaps include any wait of the device for the host)
+        jx.lib().jx_profile_begin()
+        t0 = time.perf_counter()
+        assert host_call() == 0
+        wall = time.perf_counter() - t0
+        pbuf = ctypes.create_string_buffer(4096)
+        jx.lib().jx_profile_end(pbuf, 4096)
+        e2e["split_ms"] = {k: round(float(v), 3) for k, v in
+                           (item.split("=") for item in pbuf.value.decode().split(";") if "=" in item)}
+        e2e["split_wall_ms"] = round(wall * 1e3, 3)
         e2e.update(copy_rates(V, E, weighted))
         e2e["copy_ms_at_these_rates"] = round(h2d / e2e["h2d_gbs"] / 1e6 + 4 * E / e2e["d2h_gbs"] / 1e6, 2)
         if not np.array_equal(h_out.numpy().view(np.uint32), result_bits.view(np.uint32)):

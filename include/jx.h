@@ -322,9 +322,11 @@ void jx_server_destroy(jx_server s);
 jx_status jx_csr_check(const jx_csr *g, uint32_t *flags, jx_stream_t stream);
 
 /* Per-launch timing of the fused operator on this thread: jx_profile_begin() starts
- * recording an event after each kernel the operator launches; jx_profile_end() waits for
- * them and writes "name=ms;name=ms;..." into buf (NUL-terminated, truncated to len).
- * Returns the number of timed launches.  Diagnostic only; adds event records to the stream. */
+ * recording an event after each kernel the operator launches (and, in jx_jaccard_host, after
+ * its copies in and out); jx_profile_end() waits for them and writes "name=ms;name=ms;..."
+ * into buf (NUL-terminated, truncated to len), each time measured from the previous event on
+ * the same stream.  Returns the number of timed launches.  Diagnostic only; adds event records
+ * to the stream. */
 void jx_profile_begin(void);
 int jx_profile_end(char *buf, size_t len);
 

@@ -23,6 +23,7 @@ void count_launches(uint64_t k) { tl_launches += k; }
 struct ProfMark {
   const char *name;
   cudaEvent_t ev;
+  cudaStream_t s;
 };
 static thread_local bool tl_prof = false;
 static thread_local std::vector<ProfMark> tl_marks;
@@ -32,7 +33,7 @@ void prof_mark(const char *name, cudaStream_t s) {
   cudaEvent_t ev;
   if (cudaEventCreate(&ev) != cudaSuccess) return;
   cudaEventRecord(ev, s);
-  tl_marks.push_back({name, ev});
+  tl_marks.push_back({name, ev, s});
 }
 
 int sm_count() {
@@ -180,10 +181,19 @@ int jx_profile_end(char *buf, size_t len) {
   tl_prof = false;
   std::string out;
   int count = 0;
+  // a mark's time runs from the previous mark on its own stream (from the previous mark of any
+  // stream for the first mark of a stream); marks named "_..." only anchor the next interval
   for (size_t i = 1; i < tl_marks.size(); ++i) {
+    size_t j = i - 1;
+    for (size_t k = i; k-- > 0;)
+      if (tl_marks[k].s == tl_marks[i].s) {
+        j = k;
+        break;
+      }
     float ms = 0.0f;
     cudaEventSynchronize(tl_marks[i].ev);
-    if (cudaEventElapsedTime(&ms, tl_marks[i - 1].ev, tl_marks[i].ev) != cudaSuccess) continue;
+    if (tl_marks[i].name[0] == '_') continue;
+    if (cudaEventElapsedTime(&ms, tl_marks[j].ev, tl_marks[i].ev) != cudaSuccess) continue;
     char line[160];
     snprintf(line, sizeof line, "%s%s=%.6f", count ? ";" : "", tl_marks[i].name, ms);
     out += line;
@@ -247,6 +257,7 @@ jx_status jx_jaccard_host(int32_t n, int32_t e, const int32_t *row_ptr, const in
   float *d_w = nullptr, *d_out = nullptr;
   void *d_ws = nullptr;
   cudaError_t ce;
+  prof_mark("host_call", s);
   do {
     if ((ce = cudaMallocFromPoolAsync(&d_rp, sizeof(int32_t) * ((size_t)n + 1), pool, s)) != cudaSuccess ||
         (ce = cudaMallocFromPoolAsync(&d_col, sizeof(int32_t) * (size_t)e, pool, s)) != cudaSuccess ||
@@ -262,12 +273,14 @@ jx_status jx_jaccard_host(int32_t n, int32_t e, const int32_t *row_ptr, const in
       st = set_cuda_error(ce);
       break;
     }
+    prof_mark("h2d", s);
     const jx_csr g{n, e, d_rp, d_col};
     if ((st = jx_jaccard_ws(&g, weighted ? d_w : nullptr, d_out, algo, d_ws, ws_bytes, (jx_stream_t)s)) != JX_OK) break;
     if ((ce = cudaMemcpyAsync(out_j, d_out, sizeof(float) * (size_t)e, cudaMemcpyDeviceToHost, s)) != cudaSuccess) {
       st = set_cuda_error(ce);
       break;
     }
+    prof_mark("d2h", s);
   } while (0);
   for (void *p : {(void *)d_rp, (void *)d_col, (void *)d_out, (void *)d_ws, (void *)d_w})
     if (p) cudaFreeAsync(p, s);
