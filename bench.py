@@ -513,10 +513,49 @@ def run_gpu_batched(args, world, rank, local):
     plain_ms, plain_launches, _ = timed(plain_step, max(1, args.steps // 2), 1)
     # identical results: every graph's slice of the batch equals its plain call, bit for bit
     plain_host = plain_out.cpu().numpy().view(np.uint32)
+    batch_host = np.empty(E, np.uint32)
     for b, grp in zip(batches, groups):
         lo, hi = int(eoff[grp[0]]), int(eoff[grp[-1] + 1])
-        if not np.array_equal(b.download(-1).view(np.uint32), plain_host[lo:hi]):
-            raise AssertionError("batched results differ from the per-graph calls")
+        batch_host[lo:hi] = b.download(-1).view(np.uint32)
+    if not np.array_equal(batch_host, plain_host):
+        raise AssertionError("batched results differ from the per-graph calls")
+    for b in batches:
+        b.close()
+
+    # the weighted vertex-centric path on the same batch (unit weights: every sum is an exact
+    # integer, so the values equal the unweighted ones bit for bit)
+    weighted = None
+    if not args.no_weighted_batch:
+        t = time.time()
+        ones = [np.ones(len(rp) - 1, np.float32) for rp, _, _ in graphs]
+        wbatches = [jx.Batch([(graphs[i][0], graphs[i][1], ones[i]) for i in grp], weighted=True, tune=True)
+                    for grp in groups]
+        winfos = [b.info() for b in wbatches]
+        log(f"weighted batch: built and tuned ({time.time() - t:.1f}s): " + "; ".join(i["plan"] for i in winfos))
+        wms, wlaunches, wclocks = timed(lambda: [b.run(stream) for b in wbatches], args.steps, args.warmup)
+        ones_d = [torch.from_numpy(o).cuda() for o in ones]
+        ws_w = torch.empty(max(jx.workspace_size(g, True, False) for g in plain_g), dtype=torch.uint8, device="cuda")
+
+        def plain_w_step():
+            for g, o, wd in zip(plain_g, outs, ones_d):
+                if o.numel():
+                    jx.jaccard(g, wd, o, workspace=ws_w)
+        wplain_ms, _, _ = timed(plain_w_step, max(1, args.steps // 2), 1)
+        wb = np.empty(E, np.uint32)
+        for b, grp in zip(wbatches, groups):
+            lo, hi = int(eoff[grp[0]]), int(eoff[grp[-1] + 1])
+            wb[lo:hi] = b.download(-1).view(np.uint32)
+        if not (np.array_equal(wb, plain_host) and np.array_equal(plain_out.cpu().numpy().view(np.uint32), plain_host)):
+            raise AssertionError("weighted batch (unit weights) differs from the unweighted results")
+        Bw = sum(byte_model(x["V"], x["E"], x["sum_min"], True) for x in st)
+        weighted = {"ms_per_step": round(wms, 4), "value": E * world / (wms * 1e-3), "unit": UNIT,
+                    "plans": [i["plan"] for i in winfos], "kernels_per_pass": sum(i["kernels_per_run"] for i in winfos),
+                    "gpu_launches": wlaunches, "clocks": wclocks,
+                    "plain_ms_per_step": round(wplain_ms, 3), "batched_over_plain": round(wplain_ms / wms, 3),
+                    "frac": round(Bw / (wms * 1e-3) / 1e9 / hbm_peak()[0], 4), "algorithmic_bytes": Bw,
+                    "results": "bit-identical to the unweighted batch and to the per-graph calls"}
+        for b in wbatches:
+            b.close()
 
     # end to end through the public batch API: host CSRs (pinned) in, every result out
     e2e = None
@@ -526,7 +565,7 @@ def run_gpu_batched(args, world, rank, local):
         h_out = torch.empty(E, dtype=torch.float32).pin_memory().numpy()
         def e2e_step():
             for grp in groups:
-                b = jx.Batch([pinned[i] for i in grp])
+                b = jx.Batch([pinned[i] for i in grp])  # default schedule: no tuning inside the timing
                 b.run(stream)
                 lo, hi = int(eoff[grp[0]]), int(eoff[grp[-1] + 1])
                 b.download(-1, out=h_out[lo:hi], stream=stream)
@@ -564,6 +603,7 @@ def run_gpu_batched(args, world, rank, local):
                   "gpu_launches": plain_launches,
                   "what": "one jx_jaccard_ws call per graph, graphs resident, shared workspace"},
         "batched_over_plain": round(plain_ms / ms, 3),
+        "weighted": weighted,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind,
                      "kernel": "one captured pass over every super-CSR", "algorithmic_bytes": B},
@@ -573,8 +613,18 @@ def run_gpu_batched(args, world, rank, local):
             result["cpu_baseline"] = cpu_reference_batch(graphs, st, args.cpu_seconds)
         except Exception as exc:
             result["cpu_baseline"] = {"value": None, "error": str(exc)[:200]}
-    for b in batches:
-        b.close()
+        try:  # the batch's results against the oracle on the graphs the CPU leg samples
+            order = np.argsort([x["E"] for x in st], kind="stable")
+            pick = [int(order[int(q)]) for q in np.linspace(0, len(order) - 1, 8)]
+            checks = [oracle_parity(graphs[i][0], graphs[i][1], None, False,
+                                    batch_host[int(eoff[i]):int(eoff[i + 1])].view(np.float32)) for i in pick]
+            bad = sum(c["mismatches"] for c in checks)
+            result["parity"] = {"result": ("bit-exact" if bad == 0 else f"{bad} mismatches") +
+                                          f" on {sum(c['edges_checked'] for c in checks)} edges of 8 graphs",
+                                "mismatches": bad, "graphs": pick,
+                                "oracle": "C restatement of jaccard.cpp, pinned to the reference"}
+        except Exception as exc:
+            result["parity"] = {"result": None, "error": str(exc)[:200]}
     return result
 
 
@@ -837,10 +887,12 @@ def run_gpu(args, world, rank, local):
     g = jx.GraphCSRView.from_numpy(rp, col, device=f"cuda:{local}")
     wd = torch.from_numpy(w).cuda() if weighted else None
     out = torch.empty(E, dtype=torch.float32, device="cuda")
-    ws = torch.empty(jx.workspace_size(g, weighted, args.ec), dtype=torch.uint8, device="cuda")
+    sch = json.loads(args.schedule) if args.schedule else None
+    ws_bytes = max(jx.workspace_size(g, weighted, args.ec, sch), jx.workspace_size(g, False, False, sch))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
 
-    call = lambda: jx.jaccard(g, wd, out, edge_centric=args.ec, workspace=ws)
+    call = lambda: jx.jaccard(g, wd, out, edge_centric=args.ec, workspace=ws, schedule=sch)
     ms, launches, clocks = time_calls(jx, world, local, stream, call, args.steps, args.warmup)
     result_bits = out.cpu().numpy().copy()
 
@@ -854,7 +906,6 @@ def run_gpu(args, world, rank, local):
         if "=" in item:
             k, v = item.split("=")
             kernels[k] = round(float(v), 4)
-    ksum = sum(kernels.values()) or 1.0
     dominant = max(kernels, key=kernels.get) if kernels else None
 
     # end-to-end through the host-buffer C-ABI entry point (pinned host memory)
@@ -911,14 +962,15 @@ def run_gpu(args, world, rank, local):
                           "hub/CTA/warp row kernels, fix-up)",
                 "algorithmic_bytes": B,
                 "dominant_launch": dominant,
-                "dominant_share": round(kernels.get(dominant, 0.0) / ksum, 4) if dominant else None}
+                "dominant_share": round(kernels.get(dominant, 0.0) / ms, 4) if dominant else None,
+                "dominant_share_of": "the step's event time"}
     result = {
         "metric": METRIC, "value": E * world / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": f"{args.workload}: {desc}", "algorithm": "edge_centric" if args.ec else "vertex_centric",
-                   "weighted": weighted, "V": V, "E": E, "sum_min": st["sum_min"],
+                   "weighted": weighted, "V": V, "E": E, "sum_min": st["sum_min"], "schedule": sch or "default",
                    "max_degree": st["max_degree"], "l2": l2_note(4 * (V + 1) + 4 * E + (4 * V if weighted else 0)),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "clocks": clocks, "e2e": e2e, "gpu_launches": launches, "roofline": roofline,
@@ -928,7 +980,7 @@ def run_gpu(args, world, rank, local):
     # the same graph unweighted (vertex-centric): a few more timed calls, reported beside
     unw_bits = None
     if weighted and not args.no_unweighted:
-        call_u = lambda: jx.jaccard(g, None, out, edge_centric=False, workspace=ws)
+        call_u = lambda: jx.jaccard(g, None, out, edge_centric=False, workspace=ws, schedule=sch)
         ms_u, _, clk_u = time_calls(jx, world, local, stream, call_u, 5, 2)
         unw_bits = out.cpu().numpy()
         B_u = byte_model(V, E, st["sum_min"], False)
@@ -1022,6 +1074,8 @@ def main():
     ap.add_argument("--light-requests", type=int, default=300,
                     help="served: requests of the second trace at half the sustained rate (0: skip)")
     ap.add_argument("--ec", action="store_true", help="edge-centric algorithm")
+    ap.add_argument("--schedule", default="",
+                    help='launch schedule as JSON, e.g. \'{"persistent": 1}\' (jx_schedule fields; default: the library default)')
     ap.add_argument("--permute", type=int, default=0,
                     help="R-MAT workloads: relabel the vertex ids by a bijection with this seed (0: none)")
     ap.add_argument("--unweighted", action="store_true", help="drop the vertex weights")
@@ -1029,6 +1083,7 @@ def main():
                     help="add U(0,1] vertex weights (seed 4) to a workload that has none")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-weighted-batch", action="store_true", help="batched: skip the weighted batch")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU leg (reference sample, oracle parity)")
     ap.add_argument("--no-unweighted", action="store_true",
                     help="weighted workloads: skip the unweighted calls reported beside")

@@ -92,6 +92,30 @@ jx_status jx_jaccard_ws(const jx_csr *g, const float *vertex_w, float *out_j, jx
                         void *workspace, size_t workspace_bytes, jx_stream_t stream);
 
 /*
+ * Schedule of one operator call: how the rows are split into degree bins and launched.  (This
+ * library's addition: the reference has one fixed launch shape per kernel.)  Results never
+ * depend on the schedule, only the speed does.  A zero field takes its default.
+ */
+typedef struct {
+  int32_t persistent; /* 1: one persistent launch walks the CTA, warp and lane rows; 0 (default):
+                         one kernel per bin */
+  int32_t lane_max;   /* rows of at most this many neighbours: one lane per task (1..32, default 32) */
+  int32_t warp_max;   /* ... one warp per row (lane_max..512, default 512) */
+  int32_t cta_max;    /* ... one 1024-thread CTA per row (warp_max..24576, default 24576); longer
+                         rows are split into hub work units run by 8-CTA clusters */
+  int32_t hub_unit;   /* tasks per hub work unit (default 32768) */
+  int32_t hub_batch;  /* tasks a hub warp takes per fetch (1..32, default 2) */
+  int32_t hub_beside; /* 1: the hub kernel runs on a second stream beside the row kernels;
+                         -1: before them on the call's stream; 0: the library default */
+} jx_schedule;
+
+/* jx_jaccard_ws under a given schedule (NULL: the default one), and its workspace size. */
+size_t jx_jaccard_schedule_workspace_size(const jx_csr *g, int weighted, jx_algo algo, const jx_schedule *sch);
+jx_status jx_jaccard_schedule(const jx_csr *g, const float *vertex_w, float *out_j, jx_algo algo,
+                              const jx_schedule *sch, void *workspace, size_t workspace_bytes,
+                              jx_stream_t stream);
+
+/*
  * Host-buffer form of jx_jaccard: the reference's buffers wrap host memory
  * (main.cpp:196-200), so this entry point takes host arrays, copies them to the device,
  * runs the operator and copies the results back.  Synchronous.  Pinned host memory gives
@@ -216,8 +240,10 @@ jx_status jx_csr_build(int32_t n, int64_t m, const int32_t *src, const int32_t *
  * edges and vertices in total, larger batches are split by the caller).  The graphs are
  * disjoint components, so one operator pass over the super-CSR gives each graph its own
  * results as a contiguous slice.  The pass is captured once as a CUDA graph and replayed by
- * jx_batch_run.  tune != 0 times a few grid-size plans for the degree bins on the batch and
- * keeps the fastest.  (Batching is this library's addition; the reference scores one graph
+ * jx_batch_run.  tune != 0 times candidate schedules on the batch and keeps the fastest: one
+ * kernel per degree bin against the persistent row launch, bin limits, the hub fetch cap, the
+ * hub kernel beside or before the row kernels, and the grids of the lane and warp kernels
+ * (jx_batch_info names the one kept).  (Batching is this library's addition; the reference scores one graph
  * per call.) */
 typedef struct {
   int32_t n, e;

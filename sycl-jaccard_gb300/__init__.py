@@ -76,6 +76,12 @@ class _ServerStats(ctypes.Structure):
                 ("cancelled", ctypes.c_uint64)]
 
 
+class _Schedule(ctypes.Structure):
+    _fields_ = [("persistent", ctypes.c_int32), ("lane_max", ctypes.c_int32), ("warp_max", ctypes.c_int32),
+                ("cta_max", ctypes.c_int32), ("hub_unit", ctypes.c_int32), ("hub_batch", ctypes.c_int32),
+                ("hub_beside", ctypes.c_int32)]
+
+
 class _Csr(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int32), ("e", ctypes.c_int32), ("row_ptr", ctypes.c_void_p),
                 ("col_idx", ctypes.c_void_p)]
@@ -102,6 +108,10 @@ def lib() -> ctypes.CDLL:
             "jx_jaccard_ws": ([ctypes.POINTER(_Csr), _VP, _VP, ctypes.c_int, _VP, ctypes.c_size_t, _VP], ctypes.c_int),
             "jx_jaccard_workspace_size": ([ctypes.POINTER(_Csr), ctypes.c_int, ctypes.c_int], ctypes.c_size_t),
             "jx_jaccard_host": ([i32, i32, _VP, _VP, _VP, _VP, ctypes.c_int], ctypes.c_int),
+            "jx_jaccard_schedule": ([ctypes.POINTER(_Csr), _VP, _VP, ctypes.c_int, ctypes.POINTER(_Schedule), _VP,
+                                     ctypes.c_size_t, _VP], ctypes.c_int),
+            "jx_jaccard_schedule_workspace_size": ([ctypes.POINTER(_Csr), ctypes.c_int, ctypes.c_int,
+                                                    ctypes.POINTER(_Schedule)], ctypes.c_size_t),
             "jx_host_release": ([], ctypes.c_int),
             "jx_jaccard_noalloc": ([ctypes.POINTER(_Csr), _VP, _VP, ctypes.c_int, _VP], ctypes.c_int),
             "jx_rowsum": ([i32, i32, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
@@ -211,13 +221,25 @@ class GraphCSRView:
                     self.indices.data_ptr())
 
 
+def _schedule(sch: dict | None):
+    """jx_schedule from a dict with any of its field names (missing fields: defaults)."""
+    if sch is None:
+        return None
+    unknown = set(sch) - {f for f, _ in _Schedule._fields_}
+    if unknown:
+        raise ValueError(f"unknown schedule fields {sorted(unknown)}")
+    return _Schedule(**{k: int(v) for k, v in sch.items()})
+
+
 def jaccard(graph: GraphCSRView, weights=None, result=None, edge_centric: bool = False,
-            stream=None, workspace=None):
+            stream=None, workspace=None, schedule: dict | None = None):
     """``sygraph::jaccard<edge_centric>(graph, [weights,] result, q)``.
 
     ``weights``: float32[V] device tensor of per-vertex weights, or None (unweighted).  The
     edge-centric algorithm ignores weights, as the reference does.  ``result``: float32[E]
     device tensor (allocated when None).  Asynchronous on ``stream``.  Returns ``result``.
+    ``schedule``: launch schedule (``jx_schedule`` fields: persistent, lane_max, warp_max,
+    cta_max, hub_unit, hub_batch, hub_beside); results do not depend on it.
     """
     torch = _torch()
     E = graph.number_of_edges
@@ -228,6 +250,17 @@ def jaccard(graph: GraphCSRView, weights=None, result=None, edge_centric: bool =
     algo = ALGO_EDGE_CENTRIC if edge_centric else ALGO_VERTEX_CENTRIC
     g = graph._c()
     L = lib()
+    if schedule is not None:
+        sch = _schedule(schedule)
+        if workspace is None:
+            nbytes = L.jx_jaccard_schedule_workspace_size(ctypes.byref(g), int(weights is not None), algo,
+                                                          ctypes.byref(sch))
+            workspace = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=graph.indices.device)
+        _check(L.jx_jaccard_schedule(ctypes.byref(g), wp, rp, algo, ctypes.byref(sch),
+                                     ctypes.c_void_p(workspace.data_ptr()),
+                                     workspace.numel() * workspace.element_size(), _stream(stream)),
+               "jx_jaccard_schedule")
+        return result
     if workspace is None:
         _check(L.jx_jaccard(ctypes.byref(g), wp, rp, algo, _stream(stream)), "jx_jaccard")
     else:
@@ -254,10 +287,14 @@ def jaccard_noalloc(graph: GraphCSRView, weights=None, result=None, edge_centric
     return result
 
 
-def workspace_size(graph: GraphCSRView, weighted: bool, edge_centric: bool = False) -> int:
+def workspace_size(graph: GraphCSRView, weighted: bool, edge_centric: bool = False,
+                   schedule: dict | None = None) -> int:
     g = graph._c()
-    return int(lib().jx_jaccard_workspace_size(ctypes.byref(g), int(weighted),
-                                                ALGO_EDGE_CENTRIC if edge_centric else ALGO_VERTEX_CENTRIC))
+    algo = ALGO_EDGE_CENTRIC if edge_centric else ALGO_VERTEX_CENTRIC
+    if schedule is not None:
+        return int(lib().jx_jaccard_schedule_workspace_size(ctypes.byref(g), int(weighted), algo,
+                                                             ctypes.byref(_schedule(schedule))))
+    return int(lib().jx_jaccard_workspace_size(ctypes.byref(g), int(weighted), algo))
 
 
 def jaccard_host(row_ptr: np.ndarray, col_idx: np.ndarray, weights: np.ndarray | None = None,

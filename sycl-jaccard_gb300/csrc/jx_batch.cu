@@ -6,8 +6,10 @@
 // contiguous slice of the output.  The operator's launch sequence for the super-CSR is
 // captured once as a CUDA graph and replayed by jx_batch_run, so a pass over the whole batch
 // costs one graph launch instead of one operator call (about ten kernels plus a workspace
-// allocation) per graph.  jx_batch_create can also time a few grid-size plans for the bins on
-// the batch itself and keep the fastest (the autotuner).
+// allocation) per graph.  jx_batch_create can also time candidate schedules on the batch
+// itself and keep the fastest (the autotuner): one kernel per degree bin against the persistent
+// row launch, the hub kernel beside or before the rows, bin limits, the hub fetch cap and grid
+// sizes.
 #include "jx_common.cuh"
 #include "jx_plan.h"
 
@@ -93,9 +95,12 @@ static void free_batch(jx_batch_s *b) {
 }
 
 static std::string describe(const Plan &P) {
-  char buf[160];
-  std::snprintf(buf, sizeof buf, "b0_ctas=%d b1_ctas=%d b2_ctas=%d hub_clusters=%d", P.b0_ctas, P.b1_ctas,
-                P.b2_ctas, P.hub_clusters);
+  char buf[256];
+  std::snprintf(buf, sizeof buf,
+                "%s b0_ctas=%d b1_ctas=%d b2_ctas=%d hub_clusters=%d%s lane_max=%d warp_max=%d cta_max=%d "
+                "hub_unit=%d hub_batch=%d",
+                P.persistent ? "persistent-rows" : "per-bin", P.b0_ctas, P.b1_ctas, P.b2_ctas, P.hub_clusters,
+                P.hub_beside ? " (beside)" : "", P.b0_max, P.b1_max, P.b2_max, P.hub_unit, P.hub_batch);
   return buf;
 }
 
@@ -177,17 +182,46 @@ jx_status jx_batch_create(const jx_host_graph *graphs, int32_t ngraphs, jx_algo 
   const jx_csr csr{(int32_t)b->nv, (int32_t)b->ne, b->row_ptr, b->col};
   const float *wp = b->weighted ? b->w : nullptr;
 
-  // candidate plans (the default first); the autotuner keeps the fastest on this batch
+  // candidate plans (the default first); the autotuner keeps the fastest on this batch: one
+  // kernel per bin against the persistent row launch, the hub kernel beside or before the rows,
+  // bin limits (which rows take the lane, warp, CTA or hub path), the hub fetch cap, and the
+  // grids of the lane and warp kernels
   const Plan base = fit_plan(default_plan(), b->ne, max_deg);
   std::vector<Plan> plans{base};
-  if (tune)
-    for (int m0 : {4, 8, 16})
-      for (int m1 : {2, 3, 4}) {
-        Plan P = base;
-        P.b0_ctas = sms * m0;
-        P.b1_ctas = sms * m1;
-        if (m0 != 8 || m1 != 3) plans.push_back(P);
-      }
+  if (tune) {
+    auto add = [&](Plan P) { plans.push_back(fit_plan(P, b->ne, max_deg)); };
+    Plan Q = base;
+    Q.hub_beside = !base.hub_beside;
+    add(Q);
+    Q = base;
+    Q.persistent = true;
+    add(Q);
+    for (int32_t b1 : {128, 256}) {
+      Q = base;
+      Q.b1_max = b1;
+      add(Q);
+    }
+    for (int32_t b2 : {4096, 12288}) {
+      Q = base;
+      Q.b2_max = b2;
+      add(Q);
+    }
+    for (int32_t hb : {1, 8}) {
+      Q = base;
+      Q.hub_batch = hb;
+      add(Q);
+    }
+    for (int m0 : {4, 16}) {
+      Q = base;
+      Q.b0_ctas = sms * m0;
+      add(Q);
+    }
+    for (int m1 : {2, 4}) {
+      Q = base;
+      Q.b1_ctas = sms * m1;
+      add(Q);
+    }
+  }
   size_t ws_bytes = 0;
   for (const Plan &P : plans) ws_bytes = std::max(ws_bytes, plan_workspace(csr.n, csr.e, b->weighted, P));
   JX_TRY(cudaMalloc(&b->ws, std::max<size_t>(ws_bytes, 256)));

@@ -57,11 +57,8 @@ constexpr int kCluster = 8;
 constexpr int32_t kEmpty = -1;
 constexpr int kChunk = 256;
 constexpr int kB1Cap = kB1Max / 8;   // class-stream capacity per class, B1 (exact bound)
-constexpr int kB1Warps = kRowThreads / 32;
 constexpr int kCap = (kB2Max + 7) / 8; // class-stream capacity per class, B2 (no overflow)
 constexpr int kHubCap = 8192;          // class-stream capacity per class, hubs (overflow resumes)
-constexpr int kHubTasksPerUnit = 32768;
-constexpr int kHubBatch = 2; // tasks a hub-kernel warp takes per fetch (measured best of 32/8/4/2)
 constexpr int kKeys = 128;           // plan sort keys: 4 bins x 32 log2 buckets
 constexpr unsigned kClass0 = 0x01010101u;
 
@@ -72,6 +69,8 @@ enum {
   kCtrB2 = 2 * kKeys + 8,      // work counter, B2 rows
   kCtrHub,                     // work counter, hub units
   kNumHubUnits,                // number of hub units
+  kCtrB1,                      // work counter, B1 rows (persistent kernel)
+  kCtrB0,                      // work counter, B0 rows (persistent kernel)
   kCounters = 2 * kKeys + 32
 };
 
@@ -570,23 +569,31 @@ __device__ __forceinline__ void write_task(float I, int32_t du, int32_t dv, floa
 }
 
 // ---------------------------------------------------------------- plan: degree-sorted rows
+// Degree bins of one call (a plan's choice, at most the limits of the header comment) and the
+// hub kernel's work split.
+struct Bins {
+  int32_t b0_max, b1_max, b2_max; // lane rows d <= b0_max, warp rows <= b1_max, CTA rows <= b2_max
+  int32_t hub_unit;               // tasks per hub work unit
+  int32_t hub_batch;              // tasks a hub warp takes per fetch
+};
+
 // Sort key = bin * 32 + (31 - ceil(log2 d)): hubs, then B2, B1, B0, each largest first.
-__device__ __forceinline__ int plan_key(int32_t d) {
-  const int bin = d > kB2Max ? 0 : (d > kB1Max ? 1 : (d > kB0Max ? 2 : 3));
+__device__ __forceinline__ int plan_key(int32_t d, const Bins &b) {
+  const int bin = d > b.b2_max ? 0 : (d > b.b1_max ? 1 : (d > b.b0_max ? 2 : 3));
   const int lg = d <= 1 ? 0 : 32 - __clz(d - 1);
   return bin * 32 + (31 - lg);
 }
 
 template <bool kScatter>
 __global__ void plan_kernel(int32_t n, const int32_t *__restrict__ row_ptr, int32_t *__restrict__ cnt,
-                            int32_t *__restrict__ rows) {
+                            int32_t *__restrict__ rows, Bins bins) {
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t u = base + threadIdx.x;
     int key = -1;
     if (u < n) {
       const int32_t d = __ldg(row_ptr + u + 1) - __ldg(row_ptr + u);
-      if (d > 0) key = plan_key(d);
+      if (d > 0) key = plan_key(d, bins);
     }
     const unsigned peers = __match_any_sync(kFull, key);
     if (key >= 0) {
@@ -616,9 +623,9 @@ __global__ void plan_offsets_kernel(int32_t *__restrict__ cnt) {
   cnt[kCntKeys + t] = 0;
 }
 
-// Hub work units: a hub row with d tasks gives ceil(d / kHubTasksPerUnit) units.
+// Hub work units: a hub row with d tasks gives ceil(d / hub_unit) units.
 __global__ void hub_units_kernel(const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ rows,
-                                 int32_t *__restrict__ cnt, int32_t *__restrict__ unit_off) {
+                                 int32_t *__restrict__ cnt, int32_t *__restrict__ unit_off, int32_t hub_unit) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int32_t h0 = cnt[kOffKeys + 0], h1 = cnt[kOffKeys + 32];
   int32_t run = 0;
@@ -626,7 +633,7 @@ __global__ void hub_units_kernel(const int32_t *__restrict__ row_ptr, const int3
     unit_off[i - h0] = run;
     const int32_t u = rows[i];
     const int32_t d = row_ptr[u + 1] - row_ptr[u];
-    run += (d + kHubTasksPerUnit - 1) / kHubTasksPerUnit;
+    run += (d + hub_unit - 1) / hub_unit;
   }
   unit_off[h1 - h0] = run;
   cnt[kNumHubUnits] = run;
@@ -695,7 +702,7 @@ __global__ void __launch_bounds__(1024) rowsum_long_kernel(const int32_t *__rest
       float x[8];
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
-        const int32_t p = i0 + 32 * c + lane; // du <= kB2Max: no overflow
+        const int32_t p = i0 + 32 * c + lane; // du <= kB2Max (CTA-bin rows): no overflow
         x[c] = p < du ? __ldg(w + __ldg(col + us + p)) : 0.0f;
       }
 #pragma unroll
@@ -709,62 +716,130 @@ __global__ void __launch_bounds__(1024) rowsum_long_kernel(const int32_t *__rest
 }
 
 // ---------------------------------------------------------------- B0: lane per task
+// Row u (du <= 32): its neighbours in a 64-slot hash set `t` (this warp's), then lane k runs the
+// task of neighbour k alone.
+template <bool kEC, bool kWeighted>
+__device__ __forceinline__ void lane_row(int32_t *t, int32_t u, const int32_t *__restrict__ row_ptr,
+                                         const int32_t *__restrict__ col, const float *__restrict__ w,
+                                         const float *__restrict__ S, float *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
+  const uint32_t size = 2u * kB0Max;
+  t[lane] = kEmpty;
+  t[lane + 32] = kEmpty;
+  __syncwarp();
+  if (lane < du) hset_insert(t, size, __ldg(col + us + lane));
+  __syncwarp();
+  if (lane < du) {
+    const HashProbe probe{t, size};
+    const int32_t v = __ldg(col + us + lane);
+    const int32_t vs = __ldg(row_ptr + v), dv = __ldg(row_ptr + v + 1) - vs;
+    if (dv <= du) {
+      int32_t mirror = -1;
+      float I;
+      if (!kWeighted) {
+        int32_t c = 0;
+        for (int32_t p = 0; p < dv; ++p) {
+          const int32_t x = __ldg(col + vs + p);
+          c += probe(x);
+          if (x == u) mirror = mirror == -1 ? p : -2;
+        }
+        I = (float)c;
+      } else {
+        float acc = 0.0f;
+        for (int il = 0; il < kIsILanes; ++il)
+          for (int32_t p = il; p < dv; p += kIsILanes) {
+            const int32_t x = __ldg(col + vs + p);
+            if (probe(x)) acc = __ldg(w + x) + acc;
+            if (x == u) mirror = mirror == -1 ? p : -2;
+          }
+        I = acc;
+      }
+      write_task<kEC, kWeighted>(I, du, dv, kWeighted ? __ldg(S + u) : 0.0f,
+                                 kWeighted ? __ldg(S + v) : 0.0f, (int64_t)us + lane,
+                                 mirror >= 0 ? (int64_t)vs + mirror : -1, out);
+    }
+  }
+  __syncwarp();
+}
+
 template <bool kEC, bool kWeighted>
 __global__ void __launch_bounds__(kRowThreads) b0_kernel(
     const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, const int32_t *__restrict__ cnt,
     float *__restrict__ out) {
   __shared__ int32_t tables[kRowThreads / 32][kB0Slots];
-  const int lane = threadIdx.x & 31;
-  int32_t *t = tables[threadIdx.x >> 5];
   const int32_t r0 = cnt[kOffKeys + 96], r1 = cnt[kOffKeys + 128];
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < r1; i += nwarps) {
-    const int32_t u = rows[i];
-    const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
-    const uint32_t size = 2u * kB0Max;
-    t[lane] = kEmpty;
-    t[lane + 32] = kEmpty;
-    __syncwarp();
-    if (lane < du) hset_insert(t, size, __ldg(col + us + lane));
-    __syncwarp();
-    if (lane < du) {
-      const HashProbe probe{t, size};
-      const int32_t v = __ldg(col + us + lane);
-      const int32_t vs = __ldg(row_ptr + v), dv = __ldg(row_ptr + v + 1) - vs;
-      if (dv <= du) {
-        int32_t mirror = -1;
-        float I;
-        if (!kWeighted) {
-          int32_t c = 0;
-          for (int32_t p = 0; p < dv; ++p) {
-            const int32_t x = __ldg(col + vs + p);
-            c += probe(x);
-            if (x == u) mirror = mirror == -1 ? p : -2;
-          }
-          I = (float)c;
-        } else {
-          float acc = 0.0f;
-          for (int il = 0; il < kIsILanes; ++il)
-            for (int32_t p = il; p < dv; p += kIsILanes) {
-              const int32_t x = __ldg(col + vs + p);
-              if (probe(x)) acc = __ldg(w + x) + acc;
-              if (x == u) mirror = mirror == -1 ? p : -2;
-            }
-          I = acc;
-        }
-        write_task<kEC, kWeighted>(I, du, dv, kWeighted ? __ldg(S + u) : 0.0f,
-                                   kWeighted ? __ldg(S + v) : 0.0f, (int64_t)us + lane,
-                                   mirror >= 0 ? (int64_t)vs + mirror : -1, out);
-      }
+  for (int64_t i = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < r1; i += nwarps)
+    lane_row<kEC, kWeighted>(tables[threadIdx.x >> 5], rows[i], row_ptr, col, w, S, out);
+}
+
+// ---------------------------------------------------------------- packed short tasks
+// Tasks whose list N(v) has at most W elements (W = 8 or 16), 32 / W of them per warp pass:
+// lane L works on position L % W of the (L / W)-th task of the pass (one list load and one probe
+// per lane).  A count is a segment of the ballot; a weighted sum takes the matches in the
+// reference's order (position c, c + 8, ... for class c = 0 .. 7) by shuffles inside the segment;
+// the position of u in N(v) is a segment maximum.  cand: the candidate lanes (of run_batch)
+// holding such tasks.  Built with JX_PACK_SMALL=1.
+#ifndef JX_PACK_SMALL
+#define JX_PACK_SMALL 0
+#endif
+template <bool kEC, bool kWeighted, int W, class Probe>
+__device__ __forceinline__ void run_packed(const Probe &probe, unsigned cand, const int32_t *__restrict__ col,
+                                           const float *__restrict__ w, int32_t u, int32_t us, int32_t du,
+                                           float Su, int32_t k0, int32_t vs, int32_t dv, float Sv,
+                                           float *__restrict__ out) {
+  static_assert(W == 8 || W == 16, "segment width");
+  constexpr int K = 32 / W, kPer = W / 8;
+  constexpr bool kW = kWeighted && HasWeights<Probe>::value;
+  const int lane = threadIdx.x & 31;
+  const int seg = lane / W, pos = lane % W;
+  while (cand) {
+    int b = -1; // candidate lane of this segment's task (-1: none)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int bk = cand ? __ffs(cand) - 1 : -1;
+      cand &= cand - 1;
+      if (k == seg) b = bk;
     }
-    __syncwarp();
+    const int src = b >= 0 ? b : 0;
+    const int32_t tvs = __shfl_sync(kFull, vs, src);
+    const int32_t sdv = __shfl_sync(kFull, dv, src);
+    const int32_t tdv = b >= 0 ? sdv : 0;
+    const float tSv = kWeighted ? __shfl_sync(kFull, Sv, src) : 0.0f;
+    const bool in = pos < tdv;
+    const int32_t x = in ? __ldg(col + tvs + pos) : 0; // lanes past the list probe vertex 0, a valid key
+    bool f;
+    float wv = 0.0f;
+    if constexpr (kW) f = probe.lookup(x, wv) && in; else f = probe(x) && in;
+    int32_t mp = (in && x == u) ? pos : -1;
+#pragma unroll
+    for (int o = W / 2; o >= 1; o >>= 1) mp = max(mp, __shfl_xor_sync(kFull, mp, o));
+    const unsigned fm = __ballot_sync(kFull, f);
+    float I;
+    if (!kWeighted) {
+      I = (float)__popc(fm & (((1u << W) - 1u) << (seg * W)));
+    } else {
+      const float val = f ? (kW ? wv : __ldg(w + x)) : 0.0f;
+      float acc = 0.0f;
+#pragma unroll
+      for (int s = 0; s < W; ++s) {
+        const int p = s / kPer + 8 * (s % kPer); // class-major order of positions
+        const float v = __shfl_sync(kFull, val, seg * W + p);
+        if ((fm >> (seg * W + p)) & 1u) acc = v + acc;
+      }
+      I = acc;
+    }
+    if (pos == 0 && b >= 0)
+      write_task<kEC, kWeighted>(I, du, tdv, Su, tSv, (int64_t)us + k0 + b, mp >= 0 ? (int64_t)tvs + mp : -1, out);
   }
 }
 
 // ---------------------------------------------------------------- task batches
 // Lanes fetch up to 32 candidate tasks (neighbours k0 .. k_end of row u) at once; the warp
-// then runs the ones with d_v <= d_u one by one.
+// then runs the ones with d_v <= d_u (with JX_PACK_SMALL, the short ones packed several to a
+// pass) one by one.
 template <bool kEC, bool kWeighted, class Probe, class Streams>
 __device__ __forceinline__ void run_batch(const Probe &probe, const Streams &cls,
                                           const int32_t *__restrict__ row_ptr,
@@ -781,6 +856,18 @@ __device__ __forceinline__ void run_batch(const Probe &probe, const Streams &cls
     if (kWeighted) Sv = __ldg(S + v);
   }
   unsigned todo = __ballot_sync(kFull, v >= 0 && dv <= du);
+#if JX_PACK_SMALL
+  const unsigned t8 = todo & __ballot_sync(kFull, dv <= 8);
+  if (__popc(t8) > 1) {
+    run_packed<kEC, kWeighted, 8>(probe, t8, col, w, u, us, du, Su, k0, vs, dv, Sv, out);
+    todo &= ~t8;
+  }
+  const unsigned t16 = todo & __ballot_sync(kFull, dv <= 16);
+  if (__popc(t16) > 1) {
+    run_packed<kEC, kWeighted, 16>(probe, t16, col, w, u, us, du, Su, k0, vs, dv, Sv, out);
+    todo &= ~t16;
+  }
+#endif
   while (todo) {
     const int b = __ffs(todo) - 1;
     todo &= todo - 1;
@@ -810,51 +897,60 @@ __device__ __forceinline__ uint32_t cuckoo_slots(int32_t d, uint32_t cap) {
 }
 
 // ---------------------------------------------------------------- B1: warp per row
-// Dynamic shared memory per warp: kB1Slots table slots, then (weighted) 8 * kB1Cap class-stream
-// entries.  (Folds here are short -- at most 512 matches -- and use shuffles, not a fold buffer.)
+// Shared memory of a warp: kB1Slots table slots, then (weighted) 8 * kB1Cap class-stream entries.
+// (Folds here are short -- at most 512 matches -- and use shuffles, not a fold buffer.)
+template <bool kWeighted> __host__ __device__ constexpr int b1_warp_words() {
+  return kB1Slots + (kWeighted ? 8 * kB1Cap : 0);
+}
+
+// Row u (du <= kB1Max) by one warp: cuckoo hash of N(u) in the warp's area `t`, then its tasks.
 template <bool kEC, bool kWeighted>
-__global__ void __launch_bounds__(kRowThreads) b1_kernel(
+__device__ __forceinline__ void warp_row(int32_t *t, int32_t u, const int32_t *__restrict__ row_ptr,
+                                         const int32_t *__restrict__ col, const float *__restrict__ w,
+                                         const float *__restrict__ S, float *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const SmemClassStreams cls{t + kB1Slots, kB1Cap};
+  const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
+  const float Su = kWeighted ? __ldg(S + u) : 0.0f;
+  const uint32_t slots = cuckoo_slots(du, kB1Slots);
+  int seed = 0;
+  for (; seed < kCuckooSeeds; ++seed) {
+    for (uint32_t k = lane; k < slots; k += 32) t[k] = kEmpty;
+    __syncwarp();
+    const CuckooProbe cp = cuckoo_params(t, slots, seed);
+    bool fail = false;
+    for (int32_t k = lane; k < du; k += 32) fail |= !cuckoo_insert(cp, t, __ldg(col + us + k));
+    fail = __any_sync(kFull, fail);
+    __syncwarp();
+    if (!fail) break;
+  }
+  if (seed < kCuckooSeeds) {
+    const CuckooProbe probe = cuckoo_params(t, slots, seed);
+    for (int32_t k0 = 0; k0 < du; k0 += 32)
+      run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, du, out);
+  } else { // eviction cycles with every multiplier: linear probing (load <= 0.4)
+    for (uint32_t k = lane; k < slots; k += 32) t[k] = kEmpty;
+    __syncwarp();
+    for (int32_t k = lane; k < du; k += 32) hset_insert(t, slots, __ldg(col + us + k));
+    __syncwarp();
+    const HashProbe probe{t, slots};
+    for (int32_t k0 = 0; k0 < du; k0 += 32)
+      run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, du, out);
+  }
+  __syncwarp();
+}
+
+template <bool kEC, bool kWeighted>
+__global__ void __launch_bounds__(kRowThreads, 4) b1_kernel(
     const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, const int32_t *__restrict__ cnt,
     float *__restrict__ out) {
   extern __shared__ int32_t b1_smem[];
-  constexpr int kPerWarp = kB1Slots + (kWeighted ? 8 * kB1Cap : 0);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  int32_t *t = b1_smem + wid * kPerWarp;
-  const SmemClassStreams cls{t + kB1Slots, kB1Cap};
+  int32_t *t = b1_smem + (threadIdx.x >> 5) * b1_warp_words<kWeighted>();
   const int32_t r0 = cnt[kOffKeys + 64], r1 = cnt[kOffKeys + 96];
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t i = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < r1; i += nwarps) {
-    const int32_t u = rows[i];
-    const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
-    const float Su = kWeighted ? __ldg(S + u) : 0.0f;
-    const uint32_t slots = cuckoo_slots(du, kB1Slots);
-    int seed = 0;
-    for (; seed < kCuckooSeeds; ++seed) {
-      for (uint32_t k = lane; k < slots; k += 32) t[k] = kEmpty;
-      __syncwarp();
-      const CuckooProbe cp = cuckoo_params(t, slots, seed);
-      bool fail = false;
-      for (int32_t k = lane; k < du; k += 32) fail |= !cuckoo_insert(cp, t, __ldg(col + us + k));
-      fail = __any_sync(kFull, fail);
-      __syncwarp();
-      if (!fail) break;
-    }
-    if (seed < kCuckooSeeds) {
-      const CuckooProbe probe = cuckoo_params(t, slots, seed);
-      for (int32_t k0 = 0; k0 < du; k0 += 32)
-        run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, du, out);
-    } else { // eviction cycles with every multiplier: linear probing (load <= 0.4)
-      for (uint32_t k = lane; k < slots; k += 32) t[k] = kEmpty;
-      __syncwarp();
-      for (int32_t k = lane; k < du; k += 32) hset_insert(t, slots, __ldg(col + us + k));
-      __syncwarp();
-      const HashProbe probe{t, slots};
-      for (int32_t k0 = 0; k0 < du; k0 += 32)
-        run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, du, out);
-    }
-    __syncwarp();
-  }
+  for (int64_t i = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < r1; i += nwarps)
+    warp_row<kEC, kWeighted>(t, rows[i], row_ptr, col, w, S, out);
 }
 
 // ---------------------------------------------------------------- B2: CTA per row
@@ -878,24 +974,28 @@ __device__ __forceinline__ void b2_tasks(const Probe &probe, const CS &cls, int3
   }
 }
 
+// CTA rows from the plan's list until it runs out: one row at a time per CTA, its cuckoo table in
+// `table` (kB2Slots words of shared memory), its tasks handed out to the warps.  s_row, s_task,
+// s_fail: the CTA's shared bookkeeping words.  The class streams of warp `wid` (8 classes of
+// `cap` entries) start at scratch + (blockIdx.x * 32 + wid) * 8 * cap.
 template <bool kEC, bool kWeighted, bool kExact>
-__global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
-    const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
-    const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
-    float *__restrict__ out, int32_t *__restrict__ scratch, int cap) {
-  extern __shared__ int32_t table[];
-  __shared__ int32_t s_row, s_task, s_fail;
+__device__ __forceinline__ void cta_rows_phase(int32_t *table, int32_t *s_row, int32_t *s_task, int32_t *s_fail,
+                                               const int32_t *__restrict__ row_ptr,
+                                               const int32_t *__restrict__ col, const float *__restrict__ w,
+                                               const float *__restrict__ S, const int32_t *__restrict__ rows,
+                                               int32_t *__restrict__ cnt, float *__restrict__ out,
+                                               int32_t *__restrict__ scratch, int cap) {
   const int wid = threadIdx.x >> 5;
   using CS = Streams<true, kExact>;
   const CS cls{scratch + ((int64_t)blockIdx.x * (kB2Threads / 32) + wid) * 8 * cap, cap};
   const int32_t r0 = cnt[kOffKeys + 32], r1 = cnt[kOffKeys + 64];
   for (;;) {
     if (threadIdx.x == 0) {
-      s_row = r0 + atomicAdd(cnt + kCtrB2, 1);
-      s_task = 0;
+      *s_row = r0 + atomicAdd(cnt + kCtrB2, 1);
+      *s_task = 0;
     }
     __syncthreads();
-    const int32_t i = s_row;
+    const int32_t i = *(volatile int32_t *)s_row;
     if (i >= r1) break;
     const int32_t u = rows[i];
     const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
@@ -903,14 +1003,14 @@ __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
     int seed = 0;
     for (; seed < kCuckooSeeds; ++seed) {
       for (uint32_t k = threadIdx.x; k < slots; k += blockDim.x) table[k] = kEmpty;
-      if (threadIdx.x == 0) s_fail = 0;
+      if (threadIdx.x == 0) *s_fail = 0;
       __syncthreads();
       const CuckooProbe cp = cuckoo_params(table, slots, seed);
       bool fail = false;
       for (int32_t k = threadIdx.x; k < du; k += blockDim.x) fail |= !cuckoo_insert(cp, table, __ldg(col + us + k));
-      if (fail) s_fail = 1;
+      if (fail) *s_fail = 1;
       __syncthreads();
-      const bool failed = s_fail != 0;
+      const bool failed = *(volatile int32_t *)s_fail != 0;
       __syncthreads();
       if (!failed) break;
     }
@@ -934,22 +1034,33 @@ __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
       if constexpr (kWeighted) {
         if (wtab) {
           const CuckooWProbe probe{cuckoo_params(table, slots, seed), reinterpret_cast<const float *>(table + slots)};
-          b2_tasks<kEC, kWeighted>(probe, rcls, &s_task, row_ptr, col, w, S, u, us, du, out);
+          b2_tasks<kEC, kWeighted>(probe, rcls, s_task, row_ptr, col, w, S, u, us, du, out);
         } else {
-          b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), rcls, &s_task, row_ptr, col, w, S, u, us, du, out);
+          b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), rcls, s_task, row_ptr, col, w, S, u, us, du, out);
         }
       } else {
-        b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), rcls, &s_task, row_ptr, col, w, S, u, us, du, out);
+        b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), rcls, s_task, row_ptr, col, w, S, u, us, du, out);
       }
     } else { // eviction cycles with every multiplier: linear probing (load <= 0.43)
       for (uint32_t k = threadIdx.x; k < slots; k += blockDim.x) table[k] = kEmpty;
       __syncthreads();
       for (int32_t k = threadIdx.x; k < du; k += blockDim.x) hset_insert(table, slots, __ldg(col + us + k));
       __syncthreads();
-      b2_tasks<kEC, kWeighted>(HashProbe{table, slots}, rcls, &s_task, row_ptr, col, w, S, u, us, du, out);
+      b2_tasks<kEC, kWeighted>(HashProbe{table, slots}, rcls, s_task, row_ptr, col, w, S, u, us, du, out);
     }
     __syncthreads();
   }
+}
+
+template <bool kEC, bool kWeighted, bool kExact>
+__global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
+    const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
+    const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
+    float *__restrict__ out, int32_t *__restrict__ scratch, int cap) {
+  extern __shared__ int32_t table[];
+  __shared__ int32_t s_row, s_task, s_fail;
+  cta_rows_phase<kEC, kWeighted, kExact>(table, &s_row, &s_task, &s_fail, row_ptr, col, w, S, rows, cnt, out,
+                                         scratch, cap);
 }
 
 // ---------------------------------------------------------------- hubs: 8-CTA clusters
@@ -962,7 +1073,7 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
     const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
     const int32_t *__restrict__ unit_off, uint32_t *__restrict__ bitmaps, int64_t words,
-    float *__restrict__ out, int32_t *__restrict__ scratch, int cap) {
+    float *__restrict__ out, int32_t *__restrict__ scratch, int cap, Bins bins) {
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ uint32_t filt[]; // hub_filter_words(): this CTA's filter of the unit's hub
   constexpr uint32_t kWords = hub_filter_words<kWeighted>();
@@ -995,8 +1106,8 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
     }
     const int32_t u = rows[h0 + lo];
     const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
-    const int32_t k_begin = (unit - unit_off[lo]) * kHubTasksPerUnit;
-    const int32_t k_end = min(du, k_begin + kHubTasksPerUnit);
+    const int32_t k_begin = (unit - unit_off[lo]) * bins.hub_unit;
+    const int32_t k_end = min(du, k_begin + bins.hub_unit);
     if constexpr (kWords != 0) {
       for (uint32_t k = threadIdx.x; k < kWords; k += blockDim.x) filt[k] = 0u;
       __syncthreads();
@@ -1014,9 +1125,9 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
     for (;;) {
       int32_t k0 = 0, g = 0;
       if (lane == 0) {
-        // hub tasks include whole hub-to-hub intersections: a warp takes at most kHubBatch of them
+        // hub tasks include whole hub-to-hub intersections: a warp takes at most hub_batch of them
         // at a time, so the biggest ones spread over many warps instead of queueing in one
-        g = min(kHubBatch, guided_batch(k_end - k_begin - *(volatile int32_t *)task_p, kCluster * (kHubThreads / 32)));
+        g = min(bins.hub_batch, guided_batch(k_end - k_begin - *(volatile int32_t *)task_p, kCluster * (kHubThreads / 32)));
         k0 = k_begin + atomicAdd(task_p, g);
       }
       k0 = __shfl_sync(kFull, k0, 0);
@@ -1040,6 +1151,53 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
   }
   // no CTA may exit while another can still read rank 0's shared memory
   cluster.sync();
+}
+
+// ---------------------------------------------------------------- the row bins in one launch
+// Persistent form: one 1024-thread CTA per SM, every CTA walking the bins in turn -- CTA rows,
+// then warp rows and lane rows (its 32 warps independently) -- each from a device counter, so a
+// bin's last items overlap the next bin's work instead of ending a kernel.  (Hub units stay in
+// the cluster kernel: an 8-CTA cluster needs 8 free SMs of one GPC, and a persistent grid of
+// clusters -- measured on R-MAT 24: 908 ms against 650 ms -- leaves SMs idle that CTA rows use.)
+// The shared-memory area (kB2Slots words) holds the CTA row's table, then one part per warp for
+// its warp-row table and later its lane-row table.
+constexpr int kB1Fetch = 4;  // warp rows a warp takes per fetch
+constexpr int kB0Fetch = 32; // lane rows a warp takes per fetch
+
+template <bool kEC, bool kWeighted, bool kExact>
+__global__ void __launch_bounds__(kB2Threads, 1) rows_kernel(
+    const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
+    const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
+    float *__restrict__ out, int32_t *__restrict__ scratch, int cap_b2) {
+  extern __shared__ int32_t area[];
+  __shared__ int32_t s_row, s_task, s_fail;
+  static_assert((kB2Threads / 32) * b1_warp_words<kWeighted>() <= kB2Slots, "warp-row tables");
+  cta_rows_phase<kEC, kWeighted, kExact>(area, &s_row, &s_task, &s_fail, row_ptr, col, w, S, rows, cnt, out, scratch,
+                                         cap_b2);
+  // warp rows, then lane rows: each warp in its own part of the area (no barrier between them;
+  // every thread left the CTA-row phase together)
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int32_t *t = area + wid * b1_warp_words<kWeighted>();
+  {
+    const int32_t r0 = cnt[kOffKeys + 64], r1 = cnt[kOffKeys + 96];
+    for (;;) {
+      int32_t i = 0;
+      if (lane == 0) i = r0 + atomicAdd(cnt + kCtrB1, kB1Fetch);
+      i = __shfl_sync(kFull, i, 0);
+      if (i >= r1) break;
+      for (int32_t j = i; j < min(r1, i + kB1Fetch); ++j) warp_row<kEC, kWeighted>(t, rows[j], row_ptr, col, w, S, out);
+    }
+  }
+  {
+    const int32_t r0 = cnt[kOffKeys + 96], r1 = cnt[kOffKeys + 128];
+    for (;;) {
+      int32_t i = 0;
+      if (lane == 0) i = r0 + atomicAdd(cnt + kCtrB0, kB0Fetch);
+      i = __shfl_sync(kFull, i, 0);
+      if (i >= r1) break;
+      for (int32_t j = i; j < min(r1, i + kB0Fetch); ++j) lane_row<kEC, kWeighted>(t, rows[j], row_ptr, col, w, S, out);
+    }
+  }
 }
 
 // ---------------------------------------------------------------- fix-up of uncovered edges
@@ -1133,9 +1291,48 @@ static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Grid sizes and class-stream capacities of one operator call.  The default plan fills the
 // GPU; the fixed-scratch entry point uses a small plan whose workspace fits its array.
+// Hub clusters that can be resident at once on the current device: an 8-CTA cluster of these
+// one-CTA-per-SM kernels needs 8 free SMs of one GPC, so fewer than SMs / 8 clusters may fit
+// (a cluster launched beyond them would only start when another has finished).  Both hub
+// kernel variants are asked (their shared memory differs); cached per device.
+static int resident_hub_clusters() {
+  static std::mutex mu;
+  static std::vector<int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  std::lock_guard<std::mutex> lock(mu);
+  if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
+  if (cache[dev] == 0) {
+    const int most = std::max(1, sm_count() / kCluster);
+    int fit = most;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = kCluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(most * kCluster);
+    cfg.blockDim = dim3(kHubThreads);
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    cfg.dynamicSmemBytes = sizeof(uint32_t) * hub_filter_words<false>();
+    if (cudaFuncSetAttribute(hub_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)cfg.dynamicSmemBytes) == cudaSuccess &&
+        cudaOccupancyMaxActiveClusters(&n, hub_kernel<false, false>, &cfg) == cudaSuccess && n > 0)
+      fit = std::min(fit, n);
+    cfg.dynamicSmemBytes = sizeof(uint32_t) * hub_filter_words<true>();
+    if (cudaOccupancyMaxActiveClusters(&n, hub_kernel<false, true>, &cfg) == cudaSuccess && n > 0)
+      fit = std::min(fit, n);
+    cudaGetLastError(); // a failed query leaves the SM-count bound
+    cache[dev] = fit;
+  }
+  return cache[dev];
+}
+
 Plan default_plan() {
   const int sms = sm_count();
-  Plan P{sms, sms / kCluster > 0 ? sms / kCluster : 1, kCap, kHubCap, sms * 3, sms * 8};
+  Plan P{sms, resident_hub_clusters(), kCap, kHubCap, sms * 3, sms * 8};
   P.b2_exact = true; // 8 * kCap >= kB2Max
   return P;
 }
@@ -1148,17 +1345,38 @@ Plan default_plan() {
 // maximum would let a class write past its stream.  Capacities stay multiples of 4 (int4
 // reads of a class).
 Plan fit_plan(Plan P, int64_t e, int64_t max_degree) {
+  P.b0_max = std::max(1, std::min(P.b0_max, kB0Max));
+  P.b1_max = std::max(P.b0_max, std::min(P.b1_max, kB1Max));
+  P.b2_max = std::max(P.b1_max, std::min(P.b2_max, kB2Max));
+  P.hub_unit = std::max(1, P.hub_unit);
+  P.hub_batch = std::max(1, std::min(P.hub_batch, 32));
   const int64_t bound = max_degree >= 0 ? std::min<int64_t>(max_degree, e) : e;
-  const int64_t d = std::min<int64_t>(bound, kB2Max);
+  const int64_t d = std::min<int64_t>(bound, P.b2_max);
   const int cap = (int)(((d + 7) / 8 + 3) / 4 * 4);
   P.cap_b2 = std::max(4, std::min(P.cap_b2, cap));
   P.b2_exact = 8 * (int64_t)P.cap_b2 >= d; // no CTA-bin row exceeds d edges
-  if (bound <= kB2Max) P.cap_hub = std::min(P.cap_hub, 4);
+  if (bound <= P.b2_max) P.cap_hub = std::min(P.cap_hub, 4);
   return P;
 }
 
+Plan apply_schedule(Plan P, const jx_schedule *sch, int64_t e, int64_t max_degree) {
+  if (sch) {
+    P.persistent = sch->persistent != 0;
+    if (sch->lane_max > 0) P.b0_max = sch->lane_max;
+    if (sch->warp_max > 0) P.b1_max = sch->warp_max;
+    if (sch->cta_max > 0) P.b2_max = sch->cta_max;
+    if (sch->hub_unit > 0) P.hub_unit = sch->hub_unit;
+    if (sch->hub_batch > 0) P.hub_batch = sch->hub_batch;
+    if (sch->hub_beside) P.hub_beside = sch->hub_beside > 0;
+  }
+  return fit_plan(P, e, max_degree);
+}
+
+static Bins bins_of(const Plan &P) { return Bins{P.b0_max, P.b1_max, P.b2_max, P.hub_unit, P.hub_batch}; }
+
 struct Layout {
   size_t cnt, rows, unit_off, S, scratch, bitmaps, total;
+  size_t hub_scratch; // byte offset of the hub kernel's class streams inside the scratch region
   int64_t words;
 };
 
@@ -1168,18 +1386,61 @@ static Layout layout(int32_t n, int32_t e, bool weighted_vc, const Plan &P) {
   size_t off = 0;
   L.cnt = off;      off += align256(sizeof(int32_t) * kCounters);
   L.rows = off;     off += align256(sizeof(int32_t) * (size_t)n);
-  // every hub row holds more than kB2Max edges
-  const size_t max_hubs = std::min<size_t>((size_t)n, (size_t)e / (kB2Max + 1));
+  // every hub row holds more than b2_max edges
+  const size_t max_hubs = std::min<size_t>((size_t)n, (size_t)e / ((size_t)P.b2_max + 1));
   L.unit_off = off; off += align256(sizeof(int32_t) * (max_hubs + 2));
   L.S = off;        off += weighted_vc ? align256(sizeof(float) * (size_t)n) : 0;
-  // class streams: one region per warp of the B2 grid or of the hub grid; the two kernels
-  // run one after the other and share the region
+  // class streams: one region per warp of the CTA-row grid and of the hub grid; the hub region
+  // follows the CTA-row region when the two kernels run side by side, else they share one
   const size_t b2_ids = (size_t)P.b2_ctas * (kB2Threads / 32) * 8 * P.cap_b2;
   const size_t hub_ids = (size_t)P.hub_clusters * kCluster * (kHubThreads / 32) * 8 * P.cap_hub;
-  L.scratch = off;  off += weighted_vc ? align256(sizeof(int32_t) * std::max(b2_ids, hub_ids)) : 0;
+  L.hub_scratch = P.hub_beside ? sizeof(int32_t) * b2_ids : 0;
+  L.scratch = off;
+  off += weighted_vc ? align256(sizeof(int32_t) * (P.hub_beside ? b2_ids + hub_ids : std::max(b2_ids, hub_ids))) : 0;
   L.bitmaps = off;  off += align256(sizeof(uint32_t) * (size_t)L.words * P.hub_clusters);
   L.total = off;
   return L;
+}
+
+// The second stream of a call (the hub kernel's, beside the row kernels) with its fork and join
+// events: one set per host thread and device, created on first use.  A call records `fork` on
+// its stream, makes the second stream wait for it, launches there, records `join` there and
+// makes its own stream wait for that -- also valid inside a stream capture.
+struct HubStream {
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+};
+struct HubStreams {
+  std::vector<HubStream> v;
+  ~HubStreams() {
+    for (HubStream &h : v) {
+      if (h.fork) cudaEventDestroy(h.fork);
+      if (h.join) cudaEventDestroy(h.join);
+      if (h.s) cudaStreamDestroy(h.s);
+    }
+  }
+};
+static thread_local HubStreams tl_hub_streams;
+
+static jx_status hub_stream(HubStream **out) {
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess) return set_cuda_error(ce);
+  auto &v = tl_hub_streams.v;
+  if ((int)v.size() <= dev) v.resize(dev + 1);
+  HubStream &h = v[dev];
+  if (!h.s) {
+    if ((ce = cudaStreamCreateWithFlags(&h.s, cudaStreamNonBlocking)) != cudaSuccess ||
+        (ce = cudaEventCreateWithFlags(&h.fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (ce = cudaEventCreateWithFlags(&h.join, cudaEventDisableTiming)) != cudaSuccess) {
+      if (h.fork) cudaEventDestroy(h.fork);
+      if (h.s) cudaStreamDestroy(h.s);
+      h = HubStream{};
+      return set_cuda_error(ce);
+    }
+  }
+  *out = &h;
+  return JX_OK;
 }
 
 template <bool kEC, bool kWeighted>
@@ -1202,18 +1463,19 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
   if ((ce = cudaMemsetAsync(cnt, 0, sizeof(int32_t) * kCounters, s)) != cudaSuccess) return set_cuda_error(ce);
   if ((ce = cudaMemsetAsync(bitmaps, 0, sizeof(uint32_t) * (size_t)L.words * P.hub_clusters, s)) != cudaSuccess)
     return set_cuda_error(ce);
-  plan_kernel<false><<<sms * 4, 256, 0, s>>>(n, g.row_ptr, cnt, rows);
+  const Bins bins = bins_of(P);
+  plan_kernel<false><<<sms * 4, 256, 0, s>>>(n, g.row_ptr, cnt, rows, bins);
   if ((st = check_launch()) != JX_OK) return st;
   plan_offsets_kernel<<<1, kKeys, 0, s>>>(cnt);
   if ((st = check_launch()) != JX_OK) return st;
-  plan_kernel<true><<<sms * 4, 256, 0, s>>>(n, g.row_ptr, cnt, rows);
+  plan_kernel<true><<<sms * 4, 256, 0, s>>>(n, g.row_ptr, cnt, rows, bins);
   if ((st = check_launch()) != JX_OK) return st;
-  hub_units_kernel<<<1, 32, 0, s>>>(g.row_ptr, rows, cnt, unit_off);
+  hub_units_kernel<<<1, 32, 0, s>>>(g.row_ptr, rows, cnt, unit_off, bins.hub_unit);
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("plan", s);
   if (kWeighted && !row_sums) {
-    // rows of at most kB1Max entries, then the longer ones from the plan's row lists
-    if ((st = rowsum_upto(n, g.row_ptr, g.col_idx, w, S_ws, kB1Max, s)) != JX_OK) return st;
+    // rows of the warp and lane bins, then the longer ones from the plan's row lists
+    if ((st = rowsum_upto(n, g.row_ptr, g.col_idx, w, S_ws, P.b1_max, s)) != JX_OK) return st;
     rowsum_long_kernel<<<sms, 1024, 0, s>>>(g.row_ptr, g.col_idx, w, rows, cnt, S_ws);
     if ((st = check_launch()) != JX_OK) return st;
     prof_mark("rowsum", s);
@@ -1222,7 +1484,23 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("sentinel_fill", s);
 
+  // hub units: the cluster kernel, on a second stream beside the row kernels (P.hub_beside) or
+  // first on the call's stream
+  cudaStream_t hs = s;
+  HubStream *fork = nullptr;
+  if (P.hub_beside) {
+    if ((st = hub_stream(&fork)) != JX_OK) return st;
+    hs = fork->s;
+    if ((ce = cudaEventRecord(fork->fork, s)) != cudaSuccess || (ce = cudaStreamWaitEvent(hs, fork->fork, 0)) != cudaSuccess)
+      return set_cuda_error(ce);
+    prof_mark("_fork", hs);
+  }
   {
+    cudaLaunchAttribute cluster_attr[1];
+    cluster_attr[0].id = cudaLaunchAttributeClusterDimension;
+    cluster_attr[0].val.clusterDim.x = kCluster;
+    cluster_attr[0].val.clusterDim.y = 1;
+    cluster_attr[0].val.clusterDim.z = 1;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(P.hub_clusters * kCluster);
     cfg.blockDim = dim3(kHubThreads);
@@ -1230,46 +1508,48 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
     ce = cudaFuncSetAttribute(hub_kernel<kEC, kWeighted>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)cfg.dynamicSmemBytes);
     if (ce != cudaSuccess) return set_cuda_error(ce);
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = kCluster;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
+    cfg.stream = hs;
+    cfg.attrs = cluster_attr;
     cfg.numAttrs = 1;
+    int32_t *hub_scratch = scratch ? scratch + L.hub_scratch / sizeof(int32_t) : nullptr;
     ce = cudaLaunchKernelEx(&cfg, hub_kernel<kEC, kWeighted>, (const int32_t *)g.row_ptr,
                             (const int32_t *)g.col_idx, w, (const float *)S, (const int32_t *)rows, cnt,
-                            (const int32_t *)unit_off, bitmaps, (int64_t)L.words, out, scratch, P.cap_hub);
+                            (const int32_t *)unit_off, bitmaps, (int64_t)L.words, out, hub_scratch, P.cap_hub, bins);
     if (ce != cudaSuccess) return set_cuda_error(ce);
     if ((st = check_launch()) != JX_OK) return st;
-    prof_mark("hub_rows", s);
+    prof_mark("hub_rows", hs);
   }
   const size_t smem_b2 = sizeof(int32_t) * (size_t)kB2Slots;
-  if (kWeighted && P.b2_exact) {
-    ce = cudaFuncSetAttribute(b2_kernel<kEC, kWeighted, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)smem_b2);
+  if (P.persistent) {
+    // CTA, warp and lane rows in one launch (rows_kernel)
+    auto kern = (kWeighted && P.b2_exact) ? rows_kernel<kEC, kWeighted, true> : rows_kernel<kEC, kWeighted, false>;
+    ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b2);
     if (ce != cudaSuccess) return set_cuda_error(ce);
-    b2_kernel<kEC, kWeighted, true><<<P.b2_ctas, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt,
-                                                                           out, scratch, P.cap_b2);
+    kern<<<P.b2_ctas, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out, scratch, P.cap_b2);
+    if ((st = check_launch()) != JX_OK) return st;
+    prof_mark("row_bins", s);
   } else {
-    ce = cudaFuncSetAttribute(b2_kernel<kEC, kWeighted, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)smem_b2);
+    auto b2 = (kWeighted && P.b2_exact) ? b2_kernel<kEC, kWeighted, true> : b2_kernel<kEC, kWeighted, false>;
+    ce = cudaFuncSetAttribute(b2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b2);
     if (ce != cudaSuccess) return set_cuda_error(ce);
-    b2_kernel<kEC, kWeighted, false><<<P.b2_ctas, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt,
-                                                                            out, scratch, P.cap_b2);
+    b2<<<P.b2_ctas, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out, scratch, P.cap_b2);
+    if ((st = check_launch()) != JX_OK) return st;
+    prof_mark("cta_rows", s);
+    const size_t smem_b1 = sizeof(int32_t) * (kRowThreads / 32) * b1_warp_words<kWeighted>();
+    ce = cudaFuncSetAttribute(b1_kernel<kEC, kWeighted>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b1);
+    if (ce != cudaSuccess) return set_cuda_error(ce);
+    b1_kernel<kEC, kWeighted><<<P.b1_ctas, kRowThreads, smem_b1, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
+    if ((st = check_launch()) != JX_OK) return st;
+    prof_mark("warp_rows", s);
+    b0_kernel<kEC, kWeighted><<<P.b0_ctas, kRowThreads, 0, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
+    if ((st = check_launch()) != JX_OK) return st;
+    prof_mark("lane_rows", s);
   }
-  if ((st = check_launch()) != JX_OK) return st;
-  prof_mark("cta_rows", s);
-  const size_t smem_b1 = sizeof(int32_t) * (kRowThreads / 32) * (kB1Slots + (kWeighted ? 8 * kB1Cap : 0));
-  ce = cudaFuncSetAttribute(b1_kernel<kEC, kWeighted>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b1);
-  if (ce != cudaSuccess) return set_cuda_error(ce);
-  b1_kernel<kEC, kWeighted><<<P.b1_ctas, kRowThreads, smem_b1, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
-  if ((st = check_launch()) != JX_OK) return st;
-  prof_mark("warp_rows", s);
-  b0_kernel<kEC, kWeighted><<<P.b0_ctas, kRowThreads, 0, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
-  if ((st = check_launch()) != JX_OK) return st;
-  prof_mark("lane_rows", s);
+  if (fork) {
+    if ((ce = cudaEventRecord(fork->join, hs)) != cudaSuccess || (ce = cudaStreamWaitEvent(s, fork->join, 0)) != cudaSuccess)
+      return set_cuda_error(ce);
+    prof_mark("join", s);
+  }
   fixup_kernel<kEC, kWeighted><<<sms * 8, 256, 0, s>>>(n, g.e, g.row_ptr, g.col_idx, w, S, out);
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("fixup", s);
@@ -1319,7 +1599,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[JX_NOALLOC_SCRA
 // the array: 8 B2 CTAs, one hub cluster, 1024 entries per class stream (overflows resume).
 static Plan noalloc_plan() {
   const int sms = sm_count();
-  return Plan{8, 1, 1024, 1024, sms * 3, sms * 8};
+  Plan P{8, 1, 1024, 1024, sms * 3, sms * 8};
+  P.hub_beside = false; // one stream: no second stream or events to create
+  return P;
 }
 
 // Device address of g_noalloc_scratch on the current device.  In host code the symbol names a
@@ -1399,6 +1681,30 @@ jx_status jx_jaccard_ws(const jx_csr *g, const float *vertex_w, float *out_j, jx
   if (!run) return st;
   const bool weighted = vertex_w != nullptr && algo == JX_ALGO_VERTEX_CENTRIC; // EC ignores weights
   const Plan P = fit_plan(default_plan(), g->e, -1);
+  if (!workspace || workspace_bytes < layout(g->n, g->e, weighted, P).total ||
+      (reinterpret_cast<uintptr_t>(workspace) & 255u))
+    return JX_ERR_INVALID;
+  return dispatch(*g, weighted ? vertex_w : nullptr, out_j, algo, static_cast<char *>(workspace), P,
+                  (cudaStream_t)stream);
+}
+
+size_t jx_jaccard_schedule_workspace_size(const jx_csr *g, int weighted, jx_algo algo, const jx_schedule *sch) {
+  if (!g || g->n < 0) return 0;
+  return layout(g->n, g->e, weighted && algo == JX_ALGO_VERTEX_CENTRIC,
+                apply_schedule(default_plan(), sch, g->e, -1)).total;
+}
+
+jx_status jx_jaccard_schedule(const jx_csr *g, const float *vertex_w, float *out_j, jx_algo algo,
+                              const jx_schedule *sch, void *workspace, size_t workspace_bytes,
+                              jx_stream_t stream) {
+  bool run;
+  const jx_status st = check_args(g, algo, out_j, &run);
+  if (!run) return st;
+  if (sch && (sch->lane_max < 0 || sch->warp_max < 0 || sch->cta_max < 0 || sch->hub_unit < 0 ||
+              sch->hub_batch < 0))
+    return JX_ERR_INVALID;
+  const bool weighted = vertex_w != nullptr && algo == JX_ALGO_VERTEX_CENTRIC;
+  const Plan P = apply_schedule(default_plan(), sch, g->e, -1);
   if (!workspace || workspace_bytes < layout(g->n, g->e, weighted, P).total ||
       (reinterpret_cast<uintptr_t>(workspace) & 255u))
     return JX_ERR_INVALID;

@@ -19,6 +19,19 @@ struct Plan {
   // cap_b2 holds every match of any CTA-bin task (8 * cap_b2 >= the largest CTA-bin row degree
   // the graph can have): the CTA kernel then skips the overflow bookkeeping
   bool b2_exact = false;
+  // degree bins: lane rows d <= b0_max (<= 32), warp rows d <= b1_max (<= 512), CTA rows
+  // d <= b2_max (<= 24576), hub rows above; hub rows split into work units of hub_unit tasks,
+  // a hub warp takes at most hub_batch tasks per fetch (R-MAT 24 with 32 / 8 / 4 / 2 / 1: hub
+  // kernel 293 / 214 / 198 / 188 / 186 ms weighted; 2 is the default)
+  int32_t b0_max = 32, b1_max = 512, b2_max = 24576;
+  int32_t hub_unit = 32768, hub_batch = 2;
+  // one persistent launch over the CTA, warp and lane rows on b2_ctas CTAs, instead of one
+  // kernel per bin
+  bool persistent = false;
+  // the hub kernel runs on a second stream beside the row kernels (they read the same inputs and
+  // write disjoint outputs, so CTA rows fill the SMs the hub clusters leave free); class streams
+  // then need separate regions.  Off: the kernels run one after the other on the call's stream.
+  bool hub_beside = false;
 };
 
 Plan default_plan();
@@ -26,6 +39,8 @@ Plan default_plan();
 // degree can use.  max_degree must be an upper bound of the graph's largest degree (-1:
 // unknown); results do not depend on the capacities as long as it is.
 Plan fit_plan(Plan P, int64_t e, int64_t max_degree);
+// P with the fields a schedule sets (zero fields keep P's), then fitted to the graph.
+Plan apply_schedule(Plan P, const jx_schedule *sch, int64_t e, int64_t max_degree);
 // Workspace bytes of one call under plan P.
 size_t plan_workspace(int32_t n, int32_t e, bool weighted_vc, const Plan &P);
 // The fused operator under plan P (arguments as jx_jaccard_ws; workspace >= plan_workspace).
