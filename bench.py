@@ -698,8 +698,9 @@ def run_gpu_served(args, world, rank, local):
     trace_t, trace_g = jx.graphgen.poisson_trace(args.requests, args.rate, len(res), len(up), seed=6)
     # pinned host copies of the upload pool (both arms upload from them)
     up_pinned = [tuple(torch.from_numpy(a).pin_memory().numpy() for a in g[:3]) for g in up]
+    sch = json.loads(args.schedule) if args.schedule else None
     srv = jx.Server(memory_budget=60 << 30, slots=args.slots, fold_edges=args.fold_edges,
-                    fold_max_edges=64 << 20)
+                    fold_max_edges=64 << 20, schedule=sch)
     ids = [srv.add_graph(g[0], g[1], g[2]) for g in res]
     targets = {("resident", k): ids[k] for k in range(len(res))}
     targets.update({("upload", k): up_pinned[k] for k in range(len(up))})
@@ -793,6 +794,7 @@ def run_gpu_served(args, world, rank, local):
                                f"of a resident graph (64 RMAT scale 14-20 ef 16), 30% uploads (32-graph pool, "
                                f"ER/RMAT 1e3-1e6 vertices); weighted VC, weights U(0,1]; budget 60 GB",
                    "slots": args.slots, "fold_edges": args.fold_edges, "E_trace": E_trace,
+                   "schedule": sch or "default",
                    "l2": "graphs up to 1.3 GB; consecutive requests mostly touch different graphs; no flush",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "served": {"p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),

@@ -285,6 +285,7 @@ typedef struct {
   int32_t slots;          /* passes in flight at once (>= 1), one stream and host thread each */
   int64_t fold_edges;     /* requests of at most this many edges may be folded together */
   int64_t fold_max_edges; /* edges of one folded pass at most */
+  jx_schedule schedule;   /* launch schedule of every pass (zero fields: defaults) */
 } jx_server_config;
 
 typedef struct {

@@ -58,9 +58,7 @@ class _HostGraph(ctypes.Structure):
                 ("col_idx", ctypes.c_void_p), ("vertex_w", ctypes.c_void_p)]
 
 
-class _ServerConfig(ctypes.Structure):
-    _fields_ = [("memory_budget", ctypes.c_size_t), ("slots", ctypes.c_int32), ("fold_edges", ctypes.c_int64),
-                ("fold_max_edges", ctypes.c_int64)]
+
 
 
 class _Request(ctypes.Structure):
@@ -80,6 +78,11 @@ class _Schedule(ctypes.Structure):
     _fields_ = [("persistent", ctypes.c_int32), ("lane_max", ctypes.c_int32), ("warp_max", ctypes.c_int32),
                 ("cta_max", ctypes.c_int32), ("hub_unit", ctypes.c_int32), ("hub_batch", ctypes.c_int32),
                 ("hub_beside", ctypes.c_int32)]
+
+
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("memory_budget", ctypes.c_size_t), ("slots", ctypes.c_int32), ("fold_edges", ctypes.c_int64),
+                ("fold_max_edges", ctypes.c_int64), ("schedule", _Schedule)]
 
 
 class _Csr(ctypes.Structure):
@@ -503,9 +506,9 @@ class Server:
     host array given at submit."""
 
     def __init__(self, memory_budget: int, slots: int = 4, fold_edges: int = 1 << 21,
-                 fold_max_edges: int = 1 << 26):
+                 fold_max_edges: int = 1 << 26, schedule: dict | None = None):
         _torch()  # a CUDA device must be present
-        cfg = _ServerConfig(memory_budget, slots, fold_edges, fold_max_edges)
+        cfg = _ServerConfig(memory_budget, slots, fold_edges, fold_max_edges, _schedule(schedule or {}))
         self._h = ctypes.c_void_p()
         _check(lib().jx_server_create(ctypes.byref(cfg), ctypes.byref(self._h)), "jx_server_create")
         self._keep = {}  # ticket -> host objects that must outlive the request

@@ -116,20 +116,19 @@ size_t request_bytes(const jx_server_s *S, const Req &r) {
     b += align_up(sizeof(int32_t) * ((size_t)r.n + 1)) + align_up(sizeof(int32_t) * (size_t)r.e);
     if (r.weighted) b += align_up(sizeof(float) * (size_t)r.n);
   }
-  b += align_up(plan_workspace(r.n, r.e, r.weighted, fit_plan(default_plan(), r.e, r.max_deg)));
-  (void)S;
+  b += align_up(plan_workspace(r.n, r.e, r.weighted, apply_schedule(default_plan(), &S->cfg.schedule, r.e, r.max_deg)));
   return b;
 }
 
 // The plan of a folded pass: the default grid, class streams for the largest degree in it.
-Plan fold_plan(const std::vector<Req *> &reqs, int64_t e) {
+Plan fold_plan(const jx_server_s *S, const std::vector<Req *> &reqs, int64_t e) {
   int64_t d = 0;
   for (const Req *r : reqs) d = std::max<int64_t>(d, r->max_deg);
-  return fit_plan(default_plan(), e, d);
+  return apply_schedule(default_plan(), &S->cfg.schedule, e, d);
 }
 
 // Device bytes of a folded pass over `reqs` (everything is packed, resident graphs copied).
-size_t fold_bytes(const std::vector<Req *> &reqs) {
+size_t fold_bytes(const jx_server_s *S, const std::vector<Req *> &reqs) {
   int64_t n = 0, e = 0;
   bool weighted = false;
   for (const Req *r : reqs) {
@@ -140,7 +139,7 @@ size_t fold_bytes(const std::vector<Req *> &reqs) {
   size_t b = align_up(sizeof(int32_t) * (size_t)(n + 1)) + 2 * align_up(sizeof(int32_t) * (size_t)e);
   if (weighted) b += align_up(sizeof(float) * (size_t)n);
   b += 2 * align_up(sizeof(int64_t) * (reqs.size() + 1));
-  b += align_up(plan_workspace((int32_t)n, (int32_t)e, weighted, fold_plan(reqs, e)));
+  b += align_up(plan_workspace((int32_t)n, (int32_t)e, weighted, fold_plan(S, reqs, e)));
   return b;
 }
 
@@ -188,7 +187,7 @@ struct DevBuf {
 jx_status run_single(jx_server_s *S, Req &r, cudaStream_t s) {
   if (r.e == 0) return JX_OK;
   DevBuf buf{S->pool, s, &S->inject_alloc};
-  const Plan P = fit_plan(default_plan(), r.e, r.max_deg);
+  const Plan P = apply_schedule(default_plan(), &S->cfg.schedule, r.e, r.max_deg);
   jx_csr g{r.n, r.e, nullptr, nullptr};
   const float *w = nullptr, *row_sums = nullptr;
   if (r.graph_id >= 0) {
@@ -233,7 +232,7 @@ jx_status run_fold(jx_server_s *S, std::vector<Req *> &reqs, cudaStream_t s) {
   if (ne == 0) return JX_OK;
   const bool weighted = reqs[0]->weighted;
   const jx_algo algo = reqs[0]->algo;
-  const Plan P = fold_plan(reqs, ne);
+  const Plan P = fold_plan(S, reqs, ne);
   DevBuf buf{S->pool, s, &S->inject_alloc};
   int32_t *rp = buf.get<int32_t>((size_t)nv + 1);
   int32_t *col = buf.get<int32_t>((size_t)ne);
@@ -364,7 +363,7 @@ void dispatcher_main(jx_server_s *S) {
           continue;
         }
         pass->reqs.push_back(r);
-        const size_t fb = fold_bytes(pass->reqs);
+        const size_t fb = fold_bytes(S, pass->reqs);
         if (S->resident_bytes + S->reserved + fb > budget) {
           pass->reqs.pop_back();
           break;
@@ -398,7 +397,8 @@ int64_t jx_server_clock_ns(void) { return now_ns(); }
 
 jx_status jx_server_create(const jx_server_config *cfg, jx_server *out) {
   if (!cfg || !out || cfg->slots < 1 || cfg->slots > 64 || cfg->memory_budget == 0 || cfg->fold_edges < 0 ||
-      cfg->fold_max_edges < 0)
+      cfg->fold_max_edges < 0 || cfg->schedule.lane_max < 0 || cfg->schedule.warp_max < 0 ||
+      cfg->schedule.cta_max < 0 || cfg->schedule.hub_unit < 0 || cfg->schedule.hub_batch < 0)
     return JX_ERR_INVALID;
   *out = nullptr;
   auto S = std::make_unique<jx_server_s>();

@@ -41,9 +41,11 @@ def alone(jx, g, weighted, ec):
     return jx.jaccard(view, torch.from_numpy(w).cuda() if weighted else None, edge_centric=ec).cpu().numpy()
 
 
-def test_mix_equals_alone(jx, O, pool):
+@pytest.mark.parametrize("schedule", [None, {"persistent": 1}], ids=["per-bin", "persistent"])
+def test_mix_equals_alone(jx, O, pool, schedule):
     graphs, uploads = pool
-    srv = jx.Server(memory_budget=4 << 30, slots=3, fold_edges=200_000, fold_max_edges=2_000_000)
+    srv = jx.Server(memory_budget=4 << 30, slots=3, fold_edges=200_000, fold_max_edges=2_000_000,
+                    schedule=schedule)
     ids = [srv.add_graph(*g) for g in graphs]
     rng = np.random.default_rng(9)
     reqs = []
