@@ -107,6 +107,7 @@ typedef struct {
   int32_t hub_batch;  /* tasks a hub warp takes per fetch (1..32, default 2) */
   int32_t hub_beside; /* 1: the hub kernel runs on a second stream beside the row kernels;
                          -1: before them on the call's stream; 0: the library default */
+  int32_t hub_cluster;/* CTAs per hub cluster, 4 or 8 (default 8); 0: the library default */
 } jx_schedule;
 
 /* jx_jaccard_ws under a given schedule (NULL: the default one), and its workspace size. */

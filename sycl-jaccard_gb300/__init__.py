@@ -77,7 +77,7 @@ class _ServerStats(ctypes.Structure):
 class _Schedule(ctypes.Structure):
     _fields_ = [("persistent", ctypes.c_int32), ("lane_max", ctypes.c_int32), ("warp_max", ctypes.c_int32),
                 ("cta_max", ctypes.c_int32), ("hub_unit", ctypes.c_int32), ("hub_batch", ctypes.c_int32),
-                ("hub_beside", ctypes.c_int32)]
+                ("hub_beside", ctypes.c_int32), ("hub_cluster", ctypes.c_int32)]
 
 
 class _ServerConfig(ctypes.Structure):
@@ -242,7 +242,7 @@ def jaccard(graph: GraphCSRView, weights=None, result=None, edge_centric: bool =
     edge-centric algorithm ignores weights, as the reference does.  ``result``: float32[E]
     device tensor (allocated when None).  Asynchronous on ``stream``.  Returns ``result``.
     ``schedule``: launch schedule (``jx_schedule`` fields: persistent, lane_max, warp_max,
-    cta_max, hub_unit, hub_batch, hub_beside); results do not depend on it.
+    cta_max, hub_unit, hub_batch, hub_beside, hub_cluster); results do not depend on it.
     """
     torch = _torch()
     E = graph.number_of_edges

@@ -97,10 +97,11 @@ static void free_batch(jx_batch_s *b) {
 static std::string describe(const Plan &P) {
   char buf[256];
   std::snprintf(buf, sizeof buf,
-                "%s b0_ctas=%d b1_ctas=%d b2_ctas=%d hub_clusters=%d%s lane_max=%d warp_max=%d cta_max=%d "
+                "%s b0_ctas=%d b1_ctas=%d b2_ctas=%d hub_clusters=%dx%d%s lane_max=%d warp_max=%d cta_max=%d "
                 "hub_unit=%d hub_batch=%d",
                 P.persistent ? "persistent-rows" : "per-bin", P.b0_ctas, P.b1_ctas, P.b2_ctas, P.hub_clusters,
-                P.hub_beside ? " (beside)" : "", P.b0_max, P.b1_max, P.b2_max, P.hub_unit, P.hub_batch);
+                P.hub_cluster, P.hub_beside ? " (beside)" : "", P.b0_max, P.b1_max, P.b2_max, P.hub_unit,
+                P.hub_batch);
   return buf;
 }
 
@@ -195,6 +196,10 @@ jx_status jx_batch_create(const jx_host_graph *graphs, int32_t ngraphs, jx_algo 
     add(Q);
     Q = base;
     Q.persistent = true;
+    add(Q);
+    Q = base;
+    Q.hub_cluster = base.hub_cluster == 4 ? 8 : 4;
+    Q.hub_clusters = hub_cluster_count(Q.hub_cluster);
     add(Q);
     for (int32_t b1 : {128, 256}) {
       Q = base;

@@ -775,71 +775,11 @@ __global__ void __launch_bounds__(kRowThreads) b0_kernel(
     lane_row<kEC, kWeighted>(tables[threadIdx.x >> 5], rows[i], row_ptr, col, w, S, out);
 }
 
-// ---------------------------------------------------------------- packed short tasks
-// Tasks whose list N(v) has at most W elements (W = 8 or 16), 32 / W of them per warp pass:
-// lane L works on position L % W of the (L / W)-th task of the pass (one list load and one probe
-// per lane).  A count is a segment of the ballot; a weighted sum takes the matches in the
-// reference's order (position c, c + 8, ... for class c = 0 .. 7) by shuffles inside the segment;
-// the position of u in N(v) is a segment maximum.  cand: the candidate lanes (of run_batch)
-// holding such tasks.  Built with JX_PACK_SMALL=1.
-#ifndef JX_PACK_SMALL
-#define JX_PACK_SMALL 0
-#endif
-template <bool kEC, bool kWeighted, int W, class Probe>
-__device__ __forceinline__ void run_packed(const Probe &probe, unsigned cand, const int32_t *__restrict__ col,
-                                           const float *__restrict__ w, int32_t u, int32_t us, int32_t du,
-                                           float Su, int32_t k0, int32_t vs, int32_t dv, float Sv,
-                                           float *__restrict__ out) {
-  static_assert(W == 8 || W == 16, "segment width");
-  constexpr int K = 32 / W, kPer = W / 8;
-  constexpr bool kW = kWeighted && HasWeights<Probe>::value;
-  const int lane = threadIdx.x & 31;
-  const int seg = lane / W, pos = lane % W;
-  while (cand) {
-    int b = -1; // candidate lane of this segment's task (-1: none)
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const int bk = cand ? __ffs(cand) - 1 : -1;
-      cand &= cand - 1;
-      if (k == seg) b = bk;
-    }
-    const int src = b >= 0 ? b : 0;
-    const int32_t tvs = __shfl_sync(kFull, vs, src);
-    const int32_t sdv = __shfl_sync(kFull, dv, src);
-    const int32_t tdv = b >= 0 ? sdv : 0;
-    const float tSv = kWeighted ? __shfl_sync(kFull, Sv, src) : 0.0f;
-    const bool in = pos < tdv;
-    const int32_t x = in ? __ldg(col + tvs + pos) : 0; // lanes past the list probe vertex 0, a valid key
-    bool f;
-    float wv = 0.0f;
-    if constexpr (kW) f = probe.lookup(x, wv) && in; else f = probe(x) && in;
-    int32_t mp = (in && x == u) ? pos : -1;
-#pragma unroll
-    for (int o = W / 2; o >= 1; o >>= 1) mp = max(mp, __shfl_xor_sync(kFull, mp, o));
-    const unsigned fm = __ballot_sync(kFull, f);
-    float I;
-    if (!kWeighted) {
-      I = (float)__popc(fm & (((1u << W) - 1u) << (seg * W)));
-    } else {
-      const float val = f ? (kW ? wv : __ldg(w + x)) : 0.0f;
-      float acc = 0.0f;
-#pragma unroll
-      for (int s = 0; s < W; ++s) {
-        const int p = s / kPer + 8 * (s % kPer); // class-major order of positions
-        const float v = __shfl_sync(kFull, val, seg * W + p);
-        if ((fm >> (seg * W + p)) & 1u) acc = v + acc;
-      }
-      I = acc;
-    }
-    if (pos == 0 && b >= 0)
-      write_task<kEC, kWeighted>(I, du, tdv, Su, tSv, (int64_t)us + k0 + b, mp >= 0 ? (int64_t)tvs + mp : -1, out);
-  }
-}
-
 // ---------------------------------------------------------------- task batches
 // Lanes fetch up to 32 candidate tasks (neighbours k0 .. k_end of row u) at once; the warp
-// then runs the ones with d_v <= d_u (with JX_PACK_SMALL, the short ones packed several to a
-// pass) one by one.
+// then runs the ones with d_v <= d_u one by one.  (Packing tasks of at most 8 or 16 elements 4
+// or 2 to a warp pass changed R-MAT 24 weighted by -1.5 ms and the 2000-graph batch by -0.5 %;
+// not kept.)
 template <bool kEC, bool kWeighted, class Probe, class Streams>
 __device__ __forceinline__ void run_batch(const Probe &probe, const Streams &cls,
                                           const int32_t *__restrict__ row_ptr,
@@ -856,18 +796,6 @@ __device__ __forceinline__ void run_batch(const Probe &probe, const Streams &cls
     if (kWeighted) Sv = __ldg(S + v);
   }
   unsigned todo = __ballot_sync(kFull, v >= 0 && dv <= du);
-#if JX_PACK_SMALL
-  const unsigned t8 = todo & __ballot_sync(kFull, dv <= 8);
-  if (__popc(t8) > 1) {
-    run_packed<kEC, kWeighted, 8>(probe, t8, col, w, u, us, du, Su, k0, vs, dv, Sv, out);
-    todo &= ~t8;
-  }
-  const unsigned t16 = todo & __ballot_sync(kFull, dv <= 16);
-  if (__popc(t16) > 1) {
-    run_packed<kEC, kWeighted, 16>(probe, t16, col, w, u, us, du, Su, k0, vs, dv, Sv, out);
-    todo &= ~t16;
-  }
-#endif
   while (todo) {
     const int b = __ffs(todo) - 1;
     todo &= todo - 1;
@@ -1063,12 +991,12 @@ __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
                                          scratch, cap);
 }
 
-// ---------------------------------------------------------------- hubs: 8-CTA clusters
-// A cluster takes one hub unit (hub row u, task range) at a time: its CTAs build N(u) as a
-// bitmap over [0, n) in the cluster's own global slot, all warps stream the unit's tasks
-// against it (L2 hits), then the bits are cleared again.  Cluster barriers separate the
+// ---------------------------------------------------------------- hubs: CTA clusters
+// A cluster of kCl CTAs takes one hub unit (hub row u, task range) at a time: its CTAs build
+// N(u) as a bitmap over [0, n) in the cluster's own global slot, all warps stream the unit's
+// tasks against it (L2 hits), then the bits are cleared again.  Cluster barriers separate the
 // phases; the unit index and task counter live in rank 0's shared memory.
-template <bool kEC, bool kWeighted>
+template <bool kEC, bool kWeighted, int kCl>
 __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
     const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
@@ -1080,7 +1008,7 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
   __shared__ int32_t s_unit, s_task;
   __shared__ __align__(16) float s_fold[kWeighted ? kHubThreads / 32 : 1][128];
   const unsigned rank = cluster.block_rank();
-  const int64_t cid = blockIdx.x / kCluster;
+  const int64_t cid = blockIdx.x / kCl;
   uint32_t *bm = bitmaps + cid * words;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const ClassStreams cls{scratch + ((int64_t)blockIdx.x * (kHubThreads / 32) + wid) * 8 * cap, cap,
@@ -1116,7 +1044,7 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
         atomicOr(filt + (h >> 5), 1u << (h & 31));
       }
     }
-    for (int32_t k = rank * blockDim.x + threadIdx.x; k < du; k += kCluster * blockDim.x) {
+    for (int32_t k = rank * blockDim.x + threadIdx.x; k < du; k += kCl * blockDim.x) {
       const int32_t x = __ldg(col + us + k);
       atomicOr(bm + (x >> 5), 1u << (x & 31));
     }
@@ -1127,7 +1055,7 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
       if (lane == 0) {
         // hub tasks include whole hub-to-hub intersections: a warp takes at most hub_batch of them
         // at a time, so the biggest ones spread over many warps instead of queueing in one
-        g = min(bins.hub_batch, guided_batch(k_end - k_begin - *(volatile int32_t *)task_p, kCluster * (kHubThreads / 32)));
+        g = min(bins.hub_batch, guided_batch(k_end - k_begin - *(volatile int32_t *)task_p, kCl * (kHubThreads / 32)));
         k0 = k_begin + atomicAdd(task_p, g);
       }
       k0 = __shfl_sync(kFull, k0, 0);
@@ -1141,7 +1069,7 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
                                   out);
     }
     cluster.sync();
-    for (int32_t k = rank * blockDim.x + threadIdx.x; k < du; k += kCluster * blockDim.x)
+    for (int32_t k = rank * blockDim.x + threadIdx.x; k < du; k += kCl * blockDim.x)
       __stcg(bm + (__ldg(col + us + k) >> 5), 0u);
     if (rank == 0 && threadIdx.x == 0) {
       s_unit = atomicAdd(cnt + kCtrHub, 1);
@@ -1291,48 +1219,55 @@ static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Grid sizes and class-stream capacities of one operator call.  The default plan fills the
 // GPU; the fixed-scratch entry point uses a small plan whose workspace fits its array.
-// Hub clusters that can be resident at once on the current device: an 8-CTA cluster of these
-// one-CTA-per-SM kernels needs 8 free SMs of one GPC, so fewer than SMs / 8 clusters may fit
-// (a cluster launched beyond them would only start when another has finished).  Both hub
-// kernel variants are asked (their shared memory differs); cached per device.
-static int resident_hub_clusters() {
+// Hub clusters of `cl` CTAs that can be resident at once on the current device: a cluster of
+// these one-CTA-per-SM kernels needs `cl` free SMs of one GPC, so fewer than SMs / cl clusters
+// may fit (a cluster launched beyond them would only start when another has finished; on GB300
+// 15 clusters of 8 fit, leaving 32 of 152 SMs idle).  Both hub kernel variants are asked (their
+// shared memory differs); cached per device and cluster size.
+template <int kCl> static int query_resident_clusters() {
+  const int most = std::max(1, sm_count() / kCl);
+  int fit = most;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kCl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(most * kCl);
+  cfg.blockDim = dim3(kHubThreads);
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  cfg.dynamicSmemBytes = sizeof(uint32_t) * hub_filter_words<false>();
+  if (cudaFuncSetAttribute(hub_kernel<false, false, kCl>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)cfg.dynamicSmemBytes) == cudaSuccess &&
+      cudaOccupancyMaxActiveClusters(&n, hub_kernel<false, false, kCl>, &cfg) == cudaSuccess && n > 0)
+    fit = std::min(fit, n);
+  cfg.dynamicSmemBytes = sizeof(uint32_t) * hub_filter_words<true>();
+  if (cudaOccupancyMaxActiveClusters(&n, hub_kernel<false, true, kCl>, &cfg) == cudaSuccess && n > 0)
+    fit = std::min(fit, n);
+  cudaGetLastError(); // a failed query leaves the SM-count bound
+  return fit;
+}
+
+static int resident_hub_clusters(int cl) {
   static std::mutex mu;
-  static std::vector<int> cache;
+  static std::vector<int> cache; // [device * 2 + (cl == 4)]
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 1;
   std::lock_guard<std::mutex> lock(mu);
-  if ((int)cache.size() <= dev) cache.resize(dev + 1, 0);
-  if (cache[dev] == 0) {
-    const int most = std::max(1, sm_count() / kCluster);
-    int fit = most;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = kCluster;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(most * kCluster);
-    cfg.blockDim = dim3(kHubThreads);
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    int n = 0;
-    cfg.dynamicSmemBytes = sizeof(uint32_t) * hub_filter_words<false>();
-    if (cudaFuncSetAttribute(hub_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)cfg.dynamicSmemBytes) == cudaSuccess &&
-        cudaOccupancyMaxActiveClusters(&n, hub_kernel<false, false>, &cfg) == cudaSuccess && n > 0)
-      fit = std::min(fit, n);
-    cfg.dynamicSmemBytes = sizeof(uint32_t) * hub_filter_words<true>();
-    if (cudaOccupancyMaxActiveClusters(&n, hub_kernel<false, true>, &cfg) == cudaSuccess && n > 0)
-      fit = std::min(fit, n);
-    cudaGetLastError(); // a failed query leaves the SM-count bound
-    cache[dev] = fit;
-  }
-  return cache[dev];
+  const size_t k = (size_t)dev * 2 + (cl == 4 ? 1 : 0);
+  if (cache.size() <= k) cache.resize(k + 1, 0);
+  if (cache[k] == 0) cache[k] = cl == 4 ? query_resident_clusters<4>() : query_resident_clusters<8>();
+  return cache[k];
 }
+
+int hub_cluster_count(int cluster_size) { return resident_hub_clusters(cluster_size); }
 
 Plan default_plan() {
   const int sms = sm_count();
-  Plan P{sms, resident_hub_clusters(), kCap, kHubCap, sms * 3, sms * 8};
+  Plan P{sms, resident_hub_clusters(kCluster), kCap, kHubCap, sms * 3, sms * 8};
+  P.hub_cluster = kCluster;
   P.b2_exact = true; // 8 * kCap >= kB2Max
   return P;
 }
@@ -1368,6 +1303,10 @@ Plan apply_schedule(Plan P, const jx_schedule *sch, int64_t e, int64_t max_degre
     if (sch->hub_unit > 0) P.hub_unit = sch->hub_unit;
     if (sch->hub_batch > 0) P.hub_batch = sch->hub_batch;
     if (sch->hub_beside) P.hub_beside = sch->hub_beside > 0;
+    if (sch->hub_cluster == 4 || sch->hub_cluster == 8) {
+      P.hub_cluster = sch->hub_cluster;
+      P.hub_clusters = resident_hub_clusters(P.hub_cluster);
+    }
   }
   return fit_plan(P, e, max_degree);
 }
@@ -1393,7 +1332,7 @@ static Layout layout(int32_t n, int32_t e, bool weighted_vc, const Plan &P) {
   // class streams: one region per warp of the CTA-row grid and of the hub grid; the hub region
   // follows the CTA-row region when the two kernels run side by side, else they share one
   const size_t b2_ids = (size_t)P.b2_ctas * (kB2Threads / 32) * 8 * P.cap_b2;
-  const size_t hub_ids = (size_t)P.hub_clusters * kCluster * (kHubThreads / 32) * 8 * P.cap_hub;
+  const size_t hub_ids = (size_t)P.hub_clusters * P.hub_cluster * (kHubThreads / 32) * 8 * P.cap_hub;
   L.hub_scratch = P.hub_beside ? sizeof(int32_t) * b2_ids : 0;
   L.scratch = off;
   off += weighted_vc ? align256(sizeof(int32_t) * (P.hub_beside ? b2_ids + hub_ids : std::max(b2_ids, hub_ids))) : 0;
@@ -1498,21 +1437,22 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
   {
     cudaLaunchAttribute cluster_attr[1];
     cluster_attr[0].id = cudaLaunchAttributeClusterDimension;
-    cluster_attr[0].val.clusterDim.x = kCluster;
+    const int cl = P.hub_cluster == 4 ? 4 : 8;
+    cluster_attr[0].val.clusterDim.x = cl;
     cluster_attr[0].val.clusterDim.y = 1;
     cluster_attr[0].val.clusterDim.z = 1;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(P.hub_clusters * kCluster);
+    cfg.gridDim = dim3(P.hub_clusters * cl);
     cfg.blockDim = dim3(kHubThreads);
     cfg.dynamicSmemBytes = sizeof(uint32_t) * hub_filter_words<kWeighted>();
-    ce = cudaFuncSetAttribute(hub_kernel<kEC, kWeighted>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)cfg.dynamicSmemBytes);
+    auto hub = cl == 4 ? hub_kernel<kEC, kWeighted, 4> : hub_kernel<kEC, kWeighted, 8>;
+    ce = cudaFuncSetAttribute(hub, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.dynamicSmemBytes);
     if (ce != cudaSuccess) return set_cuda_error(ce);
     cfg.stream = hs;
     cfg.attrs = cluster_attr;
     cfg.numAttrs = 1;
     int32_t *hub_scratch = scratch ? scratch + L.hub_scratch / sizeof(int32_t) : nullptr;
-    ce = cudaLaunchKernelEx(&cfg, hub_kernel<kEC, kWeighted>, (const int32_t *)g.row_ptr,
+    ce = cudaLaunchKernelEx(&cfg, hub, (const int32_t *)g.row_ptr,
                             (const int32_t *)g.col_idx, w, (const float *)S, (const int32_t *)rows, cnt,
                             (const int32_t *)unit_off, bitmaps, (int64_t)L.words, out, hub_scratch, P.cap_hub, bins);
     if (ce != cudaSuccess) return set_cuda_error(ce);

@@ -12,7 +12,7 @@ namespace jx {
 
 struct Plan {
   int b2_ctas;      // CTAs of the B2 kernel (one class-stream region per warp)
-  int hub_clusters; // 8-CTA clusters of the hub kernel (one bitmap slot each)
+  int hub_clusters; // clusters of the hub kernel (one bitmap slot each)
   int cap_b2, cap_hub;
   int b1_ctas;      // CTAs of the warp-per-row kernel
   int b0_ctas;      // CTAs of the lane-per-task kernel
@@ -32,9 +32,13 @@ struct Plan {
   // write disjoint outputs, so CTA rows fill the SMs the hub clusters leave free); class streams
   // then need separate regions.  Off: the kernels run one after the other on the call's stream.
   bool hub_beside = false;
+  // CTAs per hub cluster (4 or 8): smaller clusters fit more SMs at once, each adds a bitmap
+  int hub_cluster = 8;
 };
 
 Plan default_plan();
+// Clusters of `cluster_size` (4 or 8) hub CTAs that can be resident at once on this device.
+int hub_cluster_count(int cluster_size);
 // P with its class-stream capacities cut to what a graph of e edges and the given maximum
 // degree can use.  max_degree must be an upper bound of the graph's largest degree (-1:
 // unknown); results do not depend on the capacities as long as it is.

@@ -224,11 +224,12 @@ def test_signed_zero_and_infinite_weights(jx, O):
 SCHEDULES = [
     {"persistent": 1},
     {"hub_beside": 1},
+    {"hub_cluster": 4, "cta_max": 4096, "hub_unit": 1000},
     {"persistent": 1, "hub_beside": 1, "lane_max": 16, "warp_max": 128, "cta_max": 2048, "hub_unit": 700,
      "hub_batch": 8},
     {"persistent": 0, "hub_beside": -1, "lane_max": 8, "warp_max": 64, "cta_max": 1024, "hub_unit": 300,
      "hub_batch": 1},
-    {"persistent": 1, "hub_beside": 1, "lane_max": 1, "warp_max": 1, "cta_max": 1},  # every row a hub row
+    {"persistent": 1, "hub_beside": 1, "hub_cluster": 4, "lane_max": 1, "warp_max": 1, "cta_max": 1},  # all hub rows
 ]
 
 
