@@ -851,11 +851,14 @@ def time_calls(jx, world, local, stream, call, steps, warmup):
 
 
 def copy_rates(V, E, weighted):
-    """Host<->device copy rates of this machine for the e2e arrays (pinned host memory, one
-    cudaMemcpyAsync per array, CUDA events): GB/s for H2D of row_ptr + col (+ w) and D2H of J."""
+    """Host<->device copy rates of this machine for the e2e arrays (pinned host memory from
+    jx_host_alloc, one copy per direction, CUDA events): GB/s for H2D of row_ptr + col (+ w) and
+    D2H of J."""
     import torch
-    h_in = torch.empty(4 * (V + 1) + 4 * E + (4 * V if weighted else 0), dtype=torch.uint8).pin_memory()
-    h_out = torch.empty(4 * E, dtype=torch.uint8).pin_memory()
+    jx = importlib.import_module("sycl-jaccard_gb300")
+    ha = jx.HostArray((4 * (V + 1) + 4 * E + (4 * V if weighted else 0),), np.uint8)
+    hb = jx.HostArray((4 * E,), np.uint8)
+    h_in, h_out = torch.from_numpy(ha.array), torch.from_numpy(hb.array)
     d_in = torch.empty(h_in.numel(), dtype=torch.uint8, device="cuda")
     d_out = torch.empty(h_out.numel(), dtype=torch.uint8, device="cuda")
     s = torch.cuda.current_stream()
@@ -870,6 +873,8 @@ def copy_rates(V, E, weighted):
         torch.cuda.synchronize()
         res[name + "_gbs"] = round(3 * src.numel() / (e0.elapsed_time(e1) * 1e-3) / 1e9, 1)
     del h_in, h_out, d_in, d_out
+    ha.free()
+    hb.free()
     return res
 
 
@@ -913,15 +918,16 @@ def run_gpu(args, world, rank, local):
     # end-to-end through the host-buffer C-ABI entry point (pinned host memory)
     e2e = None
     if not args.no_e2e:
-        h_rp = torch.from_numpy(rp).pin_memory()
-        h_col = torch.from_numpy(col).pin_memory()
-        h_w = torch.from_numpy(w).pin_memory() if weighted else None
-        h_out = torch.empty(E, dtype=torch.float32).pin_memory()
+        # host arrays in pinned memory from the library's allocator (jx_host_alloc)
+        h_rp = jx.HostArray.copy_of(rp)
+        h_col = jx.HostArray.copy_of(col)
+        h_w = jx.HostArray.copy_of(w) if weighted else None
+        h_out = jx.HostArray((E,), np.float32)
         L = jx.lib()
         algo = 1 if args.ec else 0
-        host_call = lambda: L.jx_jaccard_host(V, E, h_rp.data_ptr(), h_col.data_ptr(),
-                                              h_w.data_ptr() if h_w is not None else None,
-                                              h_out.data_ptr(), algo)
+        host_call = lambda: L.jx_jaccard_host(V, E, h_rp.array.ctypes.data, h_col.array.ctypes.data,
+                                              h_w.array.ctypes.data if h_w is not None else None,
+                                              h_out.array.ctypes.data, algo)
         for _ in range(min(2, args.warmup)):
             assert host_call() == 0
         torch.cuda.synchronize()
@@ -935,7 +941,8 @@ def run_gpu(args, world, rank, local):
         h2d = 4 * (V + 1) + 4 * E + (4 * V if weighted else 0)
         e2e = {"value": E * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": 4 * E, "ms_per_step": round(e2e_s * 1e3, 3),
-               "timing": "host wall clock around the synchronous call"}
+               "timing": "host wall clock around the synchronous call",
+               "host_memory": "pinned, from jx_host_alloc"}
         # where one host call's time goes: stream events after its copies in, each kernel and
         # its copy out (event gaps include any wait of the device for the host)
         jx.lib().jx_profile_begin()
@@ -949,9 +956,11 @@ def run_gpu(args, world, rank, local):
         e2e["split_wall_ms"] = round(wall * 1e3, 3)
         e2e.update(copy_rates(V, E, weighted))
         e2e["copy_ms_at_these_rates"] = round(h2d / e2e["h2d_gbs"] / 1e6 + 4 * E / e2e["d2h_gbs"] / 1e6, 2)
-        if not np.array_equal(h_out.numpy().view(np.uint32), result_bits.view(np.uint32)):
+        if not np.array_equal(h_out.array.view(np.uint32), result_bits.view(np.uint32)):
             raise AssertionError("host-buffer entry point disagrees with the device path")
-        del h_rp, h_col, h_w, h_out
+        for h in (h_rp, h_col, h_w, h_out):
+            if h is not None:
+                h.free()
 
     B = byte_model(V, E, st["sum_min"], weighted)
     peak, peak_kind = hbm_peak()

@@ -102,12 +102,12 @@ typedef struct {
   int32_t lane_max;   /* rows of at most this many neighbours: one lane per task (1..32, default 32) */
   int32_t warp_max;   /* ... one warp per row (lane_max..512, default 512) */
   int32_t cta_max;    /* ... one 1024-thread CTA per row (warp_max..24576, default 24576); longer
-                         rows are split into hub work units run by 8-CTA clusters */
+                         rows are split into hub work units run by CTA clusters */
   int32_t hub_unit;   /* tasks per hub work unit (default 32768) */
   int32_t hub_batch;  /* tasks a hub warp takes per fetch (1..32, default 2) */
   int32_t hub_beside; /* 1: the hub kernel runs on a second stream beside the row kernels;
                          -1: before them on the call's stream; 0: the library default */
-  int32_t hub_cluster;/* CTAs per hub cluster, 4 or 8 (default 8); 0: the library default */
+  int32_t hub_cluster;/* CTAs per hub cluster, 4 or 8 (default 4); 0: the library default */
 } jx_schedule;
 
 /* jx_jaccard_ws under a given schedule (NULL: the default one), and its workspace size. */
@@ -126,6 +126,14 @@ jx_status jx_jaccard_schedule(const jx_csr *g, const float *vertex_w, float *out
  */
 jx_status jx_jaccard_host(int32_t n, int32_t e, const int32_t *row_ptr, const int32_t *col_idx,
                           const float *vertex_w, float *out_j, jx_algo algo);
+
+/* Pinned (page-locked) host memory for jx_jaccard_host's arrays, from the CUDA runtime this
+ * library uses: copies from and to it run at the host link's rate.  (Host memory pinned by other
+ * means can sit far from the GPU: on the GB300 host, arrays pinned by PyTorch uploaded at about
+ * 16 GB/s against 37 GB/s for this memory, and downloaded at 14 against 189 GB/s.)  Free with
+ * jx_host_free.  Synchronous. */
+jx_status jx_host_alloc(size_t bytes, void **ptr);
+jx_status jx_host_free(void *ptr);
 
 /* Waits for the device, then frees the device memory jx_jaccard_host keeps between calls on the
  * current device.  (The reference frees its temporaries at every call's end,

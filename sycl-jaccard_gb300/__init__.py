@@ -28,7 +28,7 @@ from . import build as _build
 from . import csrfile  # noqa: F401  (binary CSR files)
 from . import graphgen  # noqa: F401  (synthetic graphs)
 
-__all__ = ["GraphCSRView", "JxError", "jaccard", "jaccard_host", "jaccard_noalloc", "jaccard_list",
+__all__ = ["GraphCSRView", "JxError", "HostArray", "jaccard", "jaccard_host", "jaccard_noalloc", "jaccard_list",
            "count_above", "remove_reverse_edges", "csrfile", "Batch", "Server", "csr_build", "rowsum", "fill", "intersect",
            "weight", "ec_scan", "ec_unweighted", "csr_check", "lib", "launch_count",
            "launch_count_reset", "graphgen"]
@@ -116,6 +116,8 @@ def lib() -> ctypes.CDLL:
             "jx_jaccard_schedule_workspace_size": ([ctypes.POINTER(_Csr), ctypes.c_int, ctypes.c_int,
                                                     ctypes.POINTER(_Schedule)], ctypes.c_size_t),
             "jx_host_release": ([], ctypes.c_int),
+            "jx_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(_VP)], ctypes.c_int),
+            "jx_host_free": ([_VP], ctypes.c_int),
             "jx_jaccard_noalloc": ([ctypes.POINTER(_Csr), _VP, _VP, ctypes.c_int, _VP], ctypes.c_int),
             "jx_rowsum": ([i32, i32, _VP, _VP, _VP, _VP, _VP], ctypes.c_int),
             "jx_fill": ([i64, _VP, f32, _VP], ctypes.c_int),
@@ -298,6 +300,39 @@ def workspace_size(graph: GraphCSRView, weighted: bool, edge_centric: bool = Fal
         return int(lib().jx_jaccard_schedule_workspace_size(ctypes.byref(g), int(weighted), algo,
                                                              ctypes.byref(_schedule(schedule))))
     return int(lib().jx_jaccard_workspace_size(ctypes.byref(g), int(weighted), algo))
+
+
+class HostArray:
+    """A numpy array in pinned host memory from the library's runtime (jx_host_alloc), for the
+    host arrays of :func:`jaccard_host` / ``jx_jaccard_host``.  ``.array`` is the numpy view;
+    the memory is freed by :meth:`free` (or when the object is collected)."""
+
+    def __init__(self, shape, dtype):
+        dtype = np.dtype(dtype)
+        count = int(np.prod(shape))
+        p = ctypes.c_void_p()
+        _check(lib().jx_host_alloc(max(1, count * dtype.itemsize), ctypes.byref(p)), "jx_host_alloc")
+        self._p = p
+        buf = (ctypes.c_char * max(1, count * dtype.itemsize)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=dtype, count=count).reshape(shape)
+
+    @classmethod
+    def copy_of(cls, a):
+        h = cls(np.shape(a), np.asarray(a).dtype)
+        h.array[...] = a
+        return h
+
+    def free(self):
+        if self._p:
+            self.array = None
+            lib().jx_host_free(self._p)
+            self._p = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def jaccard_host(row_ptr: np.ndarray, col_idx: np.ndarray, weights: np.ndarray | None = None,

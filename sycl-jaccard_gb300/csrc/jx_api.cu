@@ -267,6 +267,7 @@ jx_status jx_jaccard_host(int32_t n, int32_t e, const int32_t *row_ptr, const in
       st = set_cuda_error(ce);
       break;
     }
+    prof_mark("alloc", s);
     if ((ce = cudaMemcpyAsync(d_rp, row_ptr, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
         (ce = cudaMemcpyAsync(d_col, col_idx, sizeof(int32_t) * (size_t)e, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
         (weighted && (ce = cudaMemcpyAsync(d_w, vertex_w, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice, s)) != cudaSuccess)) {
@@ -287,6 +288,23 @@ jx_status jx_jaccard_host(int32_t n, int32_t e, const int32_t *row_ptr, const in
   ce = cudaStreamSynchronize(s);
   if (st == JX_OK && ce != cudaSuccess) st = set_cuda_error(ce);
   return st;
+}
+
+jx_status jx_host_alloc(size_t bytes, void **ptr) {
+  if (!ptr) return JX_ERR_INVALID;
+  *ptr = nullptr;
+  const cudaError_t ce = cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocDefault);
+  if (ce != cudaSuccess) {
+    *ptr = nullptr;
+    return set_cuda_error(ce);
+  }
+  return JX_OK;
+}
+
+jx_status jx_host_free(void *ptr) {
+  if (!ptr) return JX_OK;
+  const cudaError_t ce = cudaFreeHost(ptr);
+  return ce == cudaSuccess ? JX_OK : set_cuda_error(ce);
 }
 
 jx_status jx_host_release(void) {

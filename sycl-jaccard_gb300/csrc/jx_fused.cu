@@ -17,7 +17,7 @@
 //   B0  d_u <= 32      one warp per row, one lane per task, 64-slot hash per warp
 //   B1  d_u <= 512     one warp per row, cuckoo hash of <= 1280 slots per warp (shared)
 //   B2  d_u <= 24576   one 1024-thread CTA per row, cuckoo hash of <= 58000 slots (227 KB)
-//   hub d_u >  24576   8-CTA clusters; N(u) as a bitmap over [0, n) in global memory (L2)
+//   hub d_u >  24576   4-CTA clusters; N(u) as a bitmap over [0, n) in global memory (L2)
 //
 // Streaming: a warp reads the ref list in 256-element chunks, lane k holding positions
 // k + 32j (j = 0..7): eight independent coalesced loads in flight per lane.
@@ -53,7 +53,7 @@ constexpr int kCuckooSeeds = 4;
 constexpr int kB2Threads = 1024;
 constexpr int kRowThreads = 256;
 constexpr int kHubThreads = 1024;
-constexpr int kCluster = 8;
+constexpr int kCluster = 4; // CTAs per hub cluster by default (R-MAT 24 weighted hub kernel: 4 -> 153 ms, 8 -> 189 ms)
 constexpr int32_t kEmpty = -1;
 constexpr int kChunk = 256;
 constexpr int kB1Cap = kB1Max / 8;   // class-stream capacity per class, B1 (exact bound)

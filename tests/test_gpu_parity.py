@@ -180,6 +180,13 @@ def test_host_entry_point(jx, O):
         assert jx.lib().jx_host_release() == 0
     rp2, col2 = jx.graphgen.rmat(9, 8, seed=43)  # a smaller graph in the same pool
     assert_bitwise(jx.jaccard_host(rp2, col2), O.jaccard(rp2, col2))
+    # host arrays in the library's pinned memory (jx_host_alloc / jx_host_free)
+    hrp, hcol, hw = jx.HostArray.copy_of(rp), jx.HostArray.copy_of(col), jx.HostArray.copy_of(w)
+    hout = jx.HostArray((len(col),), np.float32)
+    jx.jaccard_host(hrp.array, hcol.array, hw.array, out=hout.array)
+    assert_bitwise(hout.array, O.jaccard(rp, col, w))
+    for h in (hrp, hcol, hw, hout):
+        h.free()
 
 
 def test_csr_check(jx):
