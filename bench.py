@@ -878,6 +878,61 @@ def copy_rates(V, E, weighted):
     return res
 
 
+def e2e_worker(args):
+    """The e2e leg in a process of its own: the same graph (regenerated: the generator is a pure
+    function of its seeds), host arrays in the library's pinned memory, `e2e_steps` timed calls of
+    jx_jaccard_host (copies in, operator, copy out) after 2 untimed ones, through ctypes and the C
+    ABI only (no PyTorch in this process).  Prints one JSON line: ms per call, the split of one
+    extra call and a digest of the results."""
+    import hashlib
+    jx = importlib.import_module("sycl-jaccard_gb300")
+    threads = os.cpu_count() or 1
+    rp, col, w, _ = jx.graphgen.config_graph(args.workload, threads=threads, permute=args.permute)
+    if args.unweighted:
+        w = None
+    elif args.weighted and w is None:
+        w = jx.graphgen.uniform_weights(len(rp) - 1, seed=4, threads=threads)
+    weighted = w is not None and not args.ec
+    V, E = len(rp) - 1, len(col)
+    L = jx.lib()
+    arrs = [jx.HostArray.copy_of(rp), jx.HostArray.copy_of(col), jx.HostArray.copy_of(w) if weighted else None,
+            jx.HostArray((E,), np.float32)]
+    ptr = [a.array.ctypes.data if a is not None else None for a in arrs]
+    algo = 1 if args.ec else 0
+    call = lambda: L.jx_jaccard_host(V, E, ptr[0], ptr[1], ptr[2], ptr[3], algo)
+    for _ in range(2):
+        assert call() == 0
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        assert call() == 0
+    ms = (time.perf_counter() - t0) / args.e2e_steps * 1e3
+    L.jx_profile_begin()
+    assert call() == 0
+    pbuf = ctypes.create_string_buffer(4096)
+    L.jx_profile_end(pbuf, 4096)
+    split = {k: round(float(v), 3) for k, v in (it.split("=") for it in pbuf.value.decode().split(";") if "=" in it)}
+    digest = hashlib.sha256(arrs[3].array.view(np.uint8)).hexdigest()
+    print(json.dumps({"ms_per_step": round(ms, 3), "split_ms": split, "digest": digest}), flush=True)
+
+
+def e2e_in_worker(args, local):
+    """Run e2e_worker in a child process on this rank's GPU; returns its JSON result."""
+    env = dict(os.environ)
+    vis = env.get("CUDA_VISIBLE_DEVICES")
+    env["CUDA_VISIBLE_DEVICES"] = vis.split(",")[local] if vis else str(local)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        env.pop(k, None)
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--e2e-worker", "--workload", args.workload,
+           "--e2e-steps", str(args.e2e_steps), "--permute", str(args.permute)]
+    cmd += ["--unweighted"] if args.unweighted else []
+    cmd += ["--weighted"] if args.weighted else []
+    cmd += ["--ec"] if args.ec else []
+    r = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=900)
+    if r.returncode != 0:
+        raise RuntimeError("e2e worker failed: " + r.stderr[-500:])
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
 def run_gpu(args, world, rank, local):
     import torch
     jx = importlib.import_module("sycl-jaccard_gb300")
@@ -936,13 +991,23 @@ def run_gpu(args, world, rank, local):
             rc = host_call()
             assert rc == 0, rc
         t1 = time.perf_counter()
-        e2e_s = (t1 - t0) / args.e2e_steps
-        e2e_s = max_over_ranks(e2e_s, world)
+        in_process_s = (t1 - t0) / args.e2e_steps
         h2d = 4 * (V + 1) + 4 * E + (4 * V if weighted else 0)
+        # the headline e2e: the same call in a process of its own (C ABI through ctypes, no
+        # PyTorch), whose results must equal this run's bit for bit
+        import hashlib
+        wk = e2e_in_worker(args, local)
+        if wk["digest"] != hashlib.sha256(result_bits.view(np.uint8)).hexdigest():
+            raise AssertionError("the e2e worker's results differ from the device path")
+        e2e_s = max_over_ranks(wk["ms_per_step"] * 1e-3, world)
         e2e = {"value": E * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": 4 * E, "ms_per_step": round(e2e_s * 1e3, 3),
-               "timing": "host wall clock around the synchronous call",
-               "host_memory": "pinned, from jx_host_alloc"}
+               "timing": "host wall clock around the synchronous jx_jaccard_host call, in a process of its own "
+                         "(the same graph regenerated, ctypes + C ABI, no PyTorch); results checked bit for bit",
+               "host_memory": "pinned, from jx_host_alloc", "split_ms": wk["split_ms"],
+               "in_process": {"ms_per_step": round(max_over_ranks(in_process_s, world) * 1e3, 3),
+                              "what": "the same call in this benchmark process (PyTorch loaded, the graph's "
+                                      "arrays held): its copies run slower"}}
         # where one host call's time goes: stream events after its copies in, each kernel and
         # its copy out (event gaps include any wait of the device for the host)
         jx.lib().jx_profile_begin()
@@ -951,9 +1016,9 @@ def run_gpu(args, world, rank, local):
         wall = time.perf_counter() - t0
         pbuf = ctypes.create_string_buffer(4096)
         jx.lib().jx_profile_end(pbuf, 4096)
-        e2e["split_ms"] = {k: round(float(v), 3) for k, v in
-                           (item.split("=") for item in pbuf.value.decode().split(";") if "=" in item)}
-        e2e["split_wall_ms"] = round(wall * 1e3, 3)
+        e2e["in_process"]["split_ms"] = {k: round(float(v), 3) for k, v in
+                                         (item.split("=") for item in pbuf.value.decode().split(";") if "=" in item)}
+        e2e["in_process"]["split_wall_ms"] = round(wall * 1e3, 3)
         e2e.update(copy_rates(V, E, weighted))
         e2e["copy_ms_at_these_rates"] = round(h2d / e2e["h2d_gbs"] / 1e6 + 4 * E / e2e["d2h_gbs"] / 1e6, 2)
         if not np.array_equal(h_out.array.view(np.uint32), result_bits.view(np.uint32)):
@@ -1093,6 +1158,7 @@ def main():
     ap.add_argument("--weighted", action="store_true",
                     help="add U(0,1] vertex weights (seed 4) to a workload that has none")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-worker", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-weighted-batch", action="store_true", help="batched: skip the weighted batch")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU leg (reference sample, oracle parity)")
@@ -1103,6 +1169,9 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=150.0,
                     help="reference arm: seconds of reference samples over all timed steps")
     args = ap.parse_args()
+    if args.e2e_worker:
+        e2e_worker(args)
+        return
     if args.warmup < 3 and args.impl == "jx":
         log("warm-up raised to 3 steps")
         args.warmup = 3
