@@ -20,11 +20,13 @@ struct Plan {
   // the graph can have): the CTA kernel then skips the overflow bookkeeping
   bool b2_exact = false;
   // degree bins: lane rows d <= b0_max (<= 32), warp rows d <= b1_max (<= 512), CTA rows
-  // d <= b2_max (<= 24576), hub rows above; hub rows split into work units of hub_unit tasks,
-  // a hub warp takes at most hub_batch tasks per fetch (R-MAT 24 with 32 / 8 / 4 / 2 / 1: hub
-  // kernel 293 / 214 / 198 / 188 / 186 ms weighted; 2 is the default)
+  // d <= b2_max (<= 24576), hub rows above; hub rows split into work units of hub_unit tasks
+  // (R-MAT 24 weighted, 4-CTA clusters, units of 8192 / 32768 / 65536 / 131072 tasks: hub kernel
+  // 172 / 153 / 149 / 152 ms), a hub warp takes at most hub_batch tasks per fetch (8-CTA
+  // clusters with 32 / 8 / 4 / 2 / 1: 293 / 214 / 198 / 188 / 186 ms; 4-CTA clusters with
+  // 4 / 2 / 1: 155 / 152 / 152 ms)
   int32_t b0_max = 32, b1_max = 512, b2_max = 24576;
-  int32_t hub_unit = 32768, hub_batch = 2;
+  int32_t hub_unit = 65536, hub_batch = 2;
   // one persistent launch over the CTA, warp and lane rows on b2_ctas CTAs, instead of one
   // kernel per bin
   bool persistent = false;
