@@ -698,7 +698,9 @@ def run_gpu_served(args, world, rank, local):
     trace_t, trace_g = jx.graphgen.poisson_trace(args.requests, args.rate, len(res), len(up), seed=6)
     # pinned host copies of the upload pool (both arms upload from them)
     up_pinned = [tuple(torch.from_numpy(a).pin_memory().numpy() for a in g[:3]) for g in up]
-    sch = json.loads(args.schedule) if args.schedule else None
+    # passes run the persistent row kernel unless a schedule is given (measured: 2.05e9 edges/s
+    # against 1.99e9 per-bin with 8 slots and folding up to 8M edges)
+    sch = json.loads(args.schedule) if args.schedule else {"persistent": 1}
     srv = jx.Server(memory_budget=60 << 30, slots=args.slots, fold_edges=args.fold_edges,
                     fold_max_edges=64 << 20, schedule=sch)
     ids = [srv.add_graph(g[0], g[1], g[2]) for g in res]
@@ -1144,8 +1146,8 @@ def main():
     ap.add_argument("--workload", default="rmat24w", choices=["rmat24w", "rmat22w", "rmat20", "er4096", "batched", "served"])
     ap.add_argument("--requests", type=int, default=1000, help="served: requests in the trace")
     ap.add_argument("--rate", type=float, default=2000.0, help="served: Poisson arrival rate (1/s)")
-    ap.add_argument("--slots", type=int, default=4, help="served: passes in flight")
-    ap.add_argument("--fold-edges", type=int, default=1 << 21, help="served: fold requests up to this size")
+    ap.add_argument("--slots", type=int, default=8, help="served: passes in flight")
+    ap.add_argument("--fold-edges", type=int, default=1 << 23, help="served: fold requests up to this size")
     ap.add_argument("--max-outstanding", type=int, default=256, help="served: result buffers held at once")
     ap.add_argument("--light-requests", type=int, default=300,
                     help="served: requests of the second trace at half the sustained rate (0: skip)")
