@@ -17,6 +17,10 @@
  *   - weighted: row sums S in the reference's 32-wide scan order (jaccard.cpp:53-137) and the
  *     intersection weight I accumulated in the order a CPU SYCL device gives the reference's
  *     8 i-lanes (jaccard.cpp:343, 370-396): ref positions 0,8,16,..., then 1,9,17,..., ...
+ *     The reference adds those lanes with unordered atomics, so this is one legal schedule of
+ *     it (work-items in linear-id order, as its CPU device runs them): a runtime that schedules
+ *     the lanes differently gives other weighted results, which can differ from these by more
+ *     than 1e-6 relative (the reference order's own error against FP64 reaches 2.5e-6).
  *   - IEEE float division (no fast math).
  */
 #ifndef JX_H
