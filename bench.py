@@ -56,8 +56,8 @@ def byte_model(V, E, sum_min, weighted):
 # (workload, weighted, edge_centric); each figure carries the fingerprint of the engine sources
 # it was captured on (sources_fingerprint()) and is reported only while the sources match.
 MEASURED_TRAFFIC = {  # median over 5 calls of one capture each
-    ("rmat24w", True, False): (1329768993792, "c2b486b14077fb43"),
-    ("rmat24w", False, False): (1049481534464, "c2b486b14077fb43"),
+    ("rmat24w", True, False): (1320397623296, "d5be316c70ecf221"),
+    ("rmat24w", False, False): (1029630037248, "d5be316c70ecf221"),
 }
 
 
