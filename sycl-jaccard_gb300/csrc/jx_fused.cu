@@ -779,7 +779,13 @@ __global__ void __launch_bounds__(kRowThreads) b0_kernel(
 // Lanes fetch up to 32 candidate tasks (neighbours k0 .. k_end of row u) at once; the warp
 // then runs the ones with d_v <= d_u one by one.  (Packing tasks of at most 8 or 16 elements 4
 // or 2 to a warp pass changed R-MAT 24 weighted by -1.5 ms and the 2000-graph batch by -0.5 %;
-// not kept.)
+// not kept.  Running the tasks of at most 16 / 32 / 64 elements one per lane, 32 at once in the
+// reference's order: R-MAT 24 weighted 612 / 620 / 627 ms against 606 ms, unweighted 293 / 297 /
+// 301 against 293 ms; a 250-graph batch pass unweighted 58.2 / 58.2 / 54.2 ms against 58.5 ms,
+// weighted 126.7 (32) against 122.1 ms -- uncoalesced per-lane loads and divergence cost more
+// than the latency they hide; not kept.  Prefetching the first 2 / 4 / 8 lines of each task's
+// list to L2 when the batch is fetched: R-MAT 24 unchanged (615 / 616 / 617 against 615 ms),
+// the batch pass 1-2 % shorter; not kept.)
 template <bool kEC, bool kWeighted, class Probe, class Streams>
 __device__ __forceinline__ void run_batch(const Probe &probe, const Streams &cls,
                                           const int32_t *__restrict__ row_ptr,
