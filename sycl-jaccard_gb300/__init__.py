@@ -156,6 +156,8 @@ def lib() -> ctypes.CDLL:
             "jx_version": ([], ctypes.c_int),
             "jx_last_cuda_error": ([], ctypes.c_int),
             "jx_launch_count": ([], ctypes.c_uint64),
+            "jx_profile_begin": ([], None),
+            "jx_profile_end": ([ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
             "jx_launch_count_reset": ([], None),
         }
         for name, (args, res) in sig.items():

@@ -209,6 +209,40 @@ def test_launch_counter(jx):
     assert jx.launch_count() >= 3
 
 
+def parse_profile(L):
+    import ctypes
+    buf = ctypes.create_string_buffer(4096)
+    n = L.jx_profile_end(buf, 4096)
+    parts = [p.split("=") for p in buf.value.decode().split(";") if p]
+    return n, [(k, float(v)) for k, v in parts]
+
+
+def test_profiler(jx):
+    """jx_profile_begin/end name every timed launch of a call, with non-negative times, and
+    record nothing outside a begin/end pair."""
+    import torch
+    L = jx.lib()
+    rp, col = jx.graphgen.rmat(12, 16, seed=2)
+    w = torch.from_numpy(jx.graphgen.uniform_weights(len(rp) - 1, seed=3)).cuda()
+    g = jx.GraphCSRView.from_numpy(rp, col)
+    L.jx_profile_begin()
+    jx.jaccard(g, w)
+    n, marks = parse_profile(L)
+    names = [k for k, _ in marks]
+    assert n == len(marks) > 0
+    for k in ("plan", "rowsum", "sentinel_fill", "cta_rows", "warp_rows", "lane_rows", "fixup"):
+        assert k in names, (k, names)
+    assert all(ms >= 0.0 for _, ms in marks)
+    jx.jaccard(g, w)  # not between begin and end
+    L.jx_profile_begin()
+    jx.jaccard_host(rp, col, jx.graphgen.uniform_weights(len(rp) - 1, seed=3))
+    n, marks = parse_profile(L)
+    names = [k for k, _ in marks]
+    for k in ("h2d", "plan", "fixup", "d2h"):
+        assert k in names, (k, names)
+    assert n == len(marks)
+
+
 def test_signed_zero_and_infinite_weights(jx, O):
     """Weights of both signs over seven decades, signed zeros and a few infinities: the engine
     reproduces the reference's order bit for bit (J = NaN compared as NaN)."""
