@@ -107,7 +107,8 @@ typedef struct {
   int32_t warp_max;   /* ... one warp per row (lane_max..512, default 512) */
   int32_t cta_max;    /* ... one 1024-thread CTA per row (warp_max..24576, default 24576); longer
                          rows are split into hub work units run by CTA clusters */
-  int32_t hub_unit;   /* tasks per hub work unit (default 65536) */
+  int32_t hub_unit;   /* largest tasks per hub work unit (default 65536); units shrink, to no
+                         less than 4096 tasks, until every resident hub cluster has 4 */
   int32_t hub_batch;  /* tasks a hub warp takes per fetch (1..32, default 2) */
   int32_t hub_beside; /* 1: the hub kernel runs on a second stream beside the row kernels;
                          -1: before them on the call's stream; 0: the library default */

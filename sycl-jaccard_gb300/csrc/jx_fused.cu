@@ -71,6 +71,7 @@ enum {
   kNumHubUnits,                // number of hub units
   kCtrB1,                      // work counter, B1 rows (persistent kernel)
   kCtrB0,                      // work counter, B0 rows (persistent kernel)
+  kHubUnitSize,                // tasks per hub work unit of this call
   kCounters = 2 * kKeys + 32
 };
 
@@ -573,7 +574,7 @@ __device__ __forceinline__ void write_task(float I, int32_t du, int32_t dv, floa
 // hub kernel's work split.
 struct Bins {
   int32_t b0_max, b1_max, b2_max; // lane rows d <= b0_max, warp rows <= b1_max, CTA rows <= b2_max
-  int32_t hub_unit;               // tasks per hub work unit
+  int32_t hub_unit;               // tasks per hub work unit at most (hub_units_kernel may use fewer)
   int32_t hub_batch;              // tasks a hub warp takes per fetch
 };
 
@@ -623,20 +624,35 @@ __global__ void plan_offsets_kernel(int32_t *__restrict__ cnt) {
   cnt[kCntKeys + t] = 0;
 }
 
-// Hub work units: a hub row with d tasks gives ceil(d / hub_unit) units.
+// Hub work units: a hub row with d tasks gives ceil(d / unit) units.  unit = hub_unit, or less
+// when the hubs hold fewer than kHubUnitsPerCluster units of hub_unit tasks per cluster, so that
+// every cluster gets work (not below kHubUnitMin).  Measured: R-MAT 20 weighted has 21 hubs
+// (617,517 tasks), one unit each at 65536 -- 21 of 36 clusters busy; its hub kernel took 4.2 ms
+// against 2.8 ms with 15 clusters of 8.  R-MAT 24 (21.0M hub tasks) keeps units of 65536.
+constexpr int32_t kHubUnitsPerCluster = 4;
+constexpr int32_t kHubUnitMin = 4096;
 __global__ void hub_units_kernel(const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ rows,
-                                 int32_t *__restrict__ cnt, int32_t *__restrict__ unit_off, int32_t hub_unit) {
+                                 int32_t *__restrict__ cnt, int32_t *__restrict__ unit_off, int32_t hub_unit,
+                                 int32_t clusters) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int32_t h0 = cnt[kOffKeys + 0], h1 = cnt[kOffKeys + 32];
+  int64_t tasks = 0;
+  for (int32_t i = h0; i < h1; ++i) tasks += row_ptr[rows[i] + 1] - row_ptr[rows[i]];
+  const int64_t want = (int64_t)kHubUnitsPerCluster * (clusters > 0 ? clusters : 1);
+  const int64_t fit = (tasks + want - 1) / want;
+  const int64_t floor_unit = hub_unit < kHubUnitMin ? hub_unit : kHubUnitMin;
+  const int64_t cap_unit = fit < hub_unit ? fit : hub_unit;
+  const int32_t unit = (int32_t)(cap_unit > floor_unit ? cap_unit : floor_unit);
   int32_t run = 0;
   for (int32_t i = h0; i < h1; ++i) {
     unit_off[i - h0] = run;
     const int32_t u = rows[i];
     const int32_t d = row_ptr[u + 1] - row_ptr[u];
-    run += (d + hub_unit - 1) / hub_unit;
+    run += (d + unit - 1) / unit;
   }
   unit_off[h1 - h0] = run;
   cnt[kNumHubUnits] = run;
+  cnt[kHubUnitSize] = unit;
 }
 
 __global__ void fill_bits_kernel(int64_t n, uint32_t *__restrict__ x, uint32_t bits) {
@@ -1023,6 +1039,7 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
   int32_t *task_p = cluster.map_shared_rank(&s_task, 0);
   const int32_t h0 = cnt[kOffKeys + 0];
   const int32_t nunits = cnt[kNumHubUnits];
+  const int32_t unit_size = cnt[kHubUnitSize];
   const int32_t nhubs = cnt[kOffKeys + 32] - h0;
   if (rank == 0 && threadIdx.x == 0) {
     s_unit = atomicAdd(cnt + kCtrHub, 1);
@@ -1040,8 +1057,8 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
     }
     const int32_t u = rows[h0 + lo];
     const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
-    const int32_t k_begin = (unit - unit_off[lo]) * bins.hub_unit;
-    const int32_t k_end = min(du, k_begin + bins.hub_unit);
+    const int32_t k_begin = (unit - unit_off[lo]) * unit_size;
+    const int32_t k_end = min(du, k_begin + unit_size);
     if constexpr (kWords != 0) {
       for (uint32_t k = threadIdx.x; k < kWords; k += blockDim.x) filt[k] = 0u;
       __syncthreads();
@@ -1415,7 +1432,7 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
   if ((st = check_launch()) != JX_OK) return st;
   plan_kernel<true><<<sms * 4, 256, 0, s>>>(n, g.row_ptr, cnt, rows, bins);
   if ((st = check_launch()) != JX_OK) return st;
-  hub_units_kernel<<<1, 32, 0, s>>>(g.row_ptr, rows, cnt, unit_off, bins.hub_unit);
+  hub_units_kernel<<<1, 32, 0, s>>>(g.row_ptr, rows, cnt, unit_off, bins.hub_unit, P.hub_clusters);
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("plan", s);
   if (kWeighted && !row_sums) {
