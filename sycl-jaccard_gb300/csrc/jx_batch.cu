@@ -97,9 +97,10 @@ static void free_batch(jx_batch_s *b) {
 static std::string describe(const Plan &P) {
   char buf[256];
   std::snprintf(buf, sizeof buf,
-                "%s b0_ctas=%d b1_ctas=%d b2_ctas=%d hub_clusters=%dx%d%s lane_max=%d warp_max=%d cta_max=%d "
+                "%s b0_ctas=%d b1_ctas=%s b2_ctas=%d hub_clusters=%dx%d%s lane_max=%d warp_max=%d cta_max=%d "
                 "hub_unit=%d hub_batch=%d",
-                P.persistent ? "persistent-rows" : "per-bin", P.b0_ctas, P.b1_ctas, P.b2_ctas, P.hub_clusters,
+                P.persistent ? "persistent-rows" : "per-bin", P.b0_ctas,
+                P.b1_ctas > 0 ? std::to_string(P.b1_ctas).c_str() : "resident", P.b2_ctas, P.hub_clusters,
                 P.hub_cluster, P.hub_beside ? " (beside)" : "", P.b0_max, P.b1_max, P.b2_max, P.hub_unit,
                 P.hub_batch);
   return buf;

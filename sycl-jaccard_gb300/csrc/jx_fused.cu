@@ -1289,7 +1289,7 @@ int hub_cluster_count(int cluster_size) { return resident_hub_clusters(cluster_s
 
 Plan default_plan() {
   const int sms = sm_count();
-  Plan P{sms, resident_hub_clusters(kCluster), kCap, kHubCap, sms * 3, sms * 8};
+  Plan P{sms, resident_hub_clusters(kCluster), kCap, kHubCap, 0, sms * 8}; // b1_ctas 0: by occupancy
   P.hub_cluster = kCluster;
   P.b2_exact = true; // 8 * kCap >= kB2Max
   return P;
@@ -1501,7 +1501,14 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
     const size_t smem_b1 = sizeof(int32_t) * (kRowThreads / 32) * b1_warp_words<kWeighted>();
     ce = cudaFuncSetAttribute(b1_kernel<kEC, kWeighted>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b1);
     if (ce != cudaSuccess) return set_cuda_error(ce);
-    b1_kernel<kEC, kWeighted><<<P.b1_ctas, kRowThreads, smem_b1, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
+    int b1_grid = P.b1_ctas;
+    if (b1_grid <= 0) { // every CTA that fits at once: 4 per SM unweighted, 3 weighted (shared memory)
+      int per_sm = 0;
+      ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b1_kernel<kEC, kWeighted>, kRowThreads, smem_b1);
+      if (ce != cudaSuccess) return set_cuda_error(ce);
+      b1_grid = std::max(1, per_sm) * sms;
+    }
+    b1_kernel<kEC, kWeighted><<<b1_grid, kRowThreads, smem_b1, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
     if ((st = check_launch()) != JX_OK) return st;
     prof_mark("warp_rows", s);
     b0_kernel<kEC, kWeighted><<<P.b0_ctas, kRowThreads, 0, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);

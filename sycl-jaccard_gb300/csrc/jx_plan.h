@@ -14,7 +14,7 @@ struct Plan {
   int b2_ctas;      // CTAs of the B2 kernel (one class-stream region per warp)
   int hub_clusters; // clusters of the hub kernel (one bitmap slot each)
   int cap_b2, cap_hub;
-  int b1_ctas;      // CTAs of the warp-per-row kernel
+  int b1_ctas;      // CTAs of the warp-per-row kernel (0: as many as fit on the GPU at once)
   int b0_ctas;      // CTAs of the lane-per-task kernel
   // cap_b2 holds every match of any CTA-bin task (8 * cap_b2 >= the largest CTA-bin row degree
   // the graph can have): the CTA kernel then skips the overflow bookkeeping
