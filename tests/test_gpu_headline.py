@@ -4,7 +4,7 @@ R-MAT scale 24, edge factor 16, (a,b,c,d) = (.57,.19,.19,.05), seed 3, vertex we
 seed 4 (V = 16,777,216, E = 520,759,968): the graph every headline number is measured on.
 The whole output is far too large for the oracle, so it is compared on sampled row ranges
 (oracle.check_rows): the five largest hubs -- rows of up to 406,291 neighbours whose tasks are
-split into hub work units of 32,768 tasks and whose hub-to-hub intersections of more than
+split into hub work units (of 65,536 tasks on this graph) and whose hub-to-hub intersections of more than
 65,536 matches overflow the 8,192-entry class streams and resume from the adjacency list --,
 the row of degree nearest 21,000 (a CTA row whose hash table leaves no room for slot weights),
 a band of 2,000 rows in the middle of the id range and the last 3,000 rows.  Weighted VC,
@@ -35,7 +35,7 @@ def test_headline_exercises_hub_units_and_overflow(O, headline):
     d = np.diff(rp.astype(np.int64))
     ranges = O.check_rows(rp)
     hub0 = ranges[0][1]
-    assert d[hub0] > 32768  # more tasks than one hub work unit
+    assert d[hub0] > 65536  # more tasks than one hub work unit
     c = O.counts(rp, col, rows=(hub0, hub0 + 1))
     assert c.max() > 8 * 8192  # some class of that task holds more than a hub class stream
     cta = ranges[5][1]
