@@ -113,6 +113,11 @@ typedef struct {
   int32_t hub_beside; /* 1: the hub kernel runs on a second stream beside the row kernels;
                          -1: before them on the call's stream; 0: the library default */
   int32_t hub_cluster;/* CTAs per hub cluster, 4 or 8 (default 4); 0: the library default */
+  int32_t relabel;    /* 1: the row kernels work on vertex ids renumbered by degree (high-degree
+                         vertices first; the lists stay in place, their entries mapped), at the
+                         cost of a copy of col_idx in the workspace -- faster on graphs whose own
+                         ids scatter the high-degree vertices; -1 or 0 (default): the graph's
+                         own ids */
 } jx_schedule;
 
 /* jx_jaccard_ws under a given schedule (NULL: the default one), and its workspace size. */

@@ -77,7 +77,7 @@ class _ServerStats(ctypes.Structure):
 class _Schedule(ctypes.Structure):
     _fields_ = [("persistent", ctypes.c_int32), ("lane_max", ctypes.c_int32), ("warp_max", ctypes.c_int32),
                 ("cta_max", ctypes.c_int32), ("hub_unit", ctypes.c_int32), ("hub_batch", ctypes.c_int32),
-                ("hub_beside", ctypes.c_int32), ("hub_cluster", ctypes.c_int32)]
+                ("hub_beside", ctypes.c_int32), ("hub_cluster", ctypes.c_int32), ("relabel", ctypes.c_int32)]
 
 
 class _ServerConfig(ctypes.Structure):

@@ -98,11 +98,11 @@ static std::string describe(const Plan &P) {
   char buf[256];
   std::snprintf(buf, sizeof buf,
                 "%s b0_ctas=%d b1_ctas=%s b2_ctas=%d hub_clusters=%dx%d%s lane_max=%d warp_max=%d cta_max=%d "
-                "hub_unit=%d hub_batch=%d",
+                "hub_unit=%d hub_batch=%d%s",
                 P.persistent ? "persistent-rows" : "per-bin", P.b0_ctas,
                 P.b1_ctas > 0 ? std::to_string(P.b1_ctas).c_str() : "resident", P.b2_ctas, P.hub_clusters,
                 P.hub_cluster, P.hub_beside ? " (beside)" : "", P.b0_max, P.b1_max, P.b2_max, P.hub_unit,
-                P.hub_batch);
+                P.hub_batch, P.relabel ? " relabelled" : "");
   return buf;
 }
 
@@ -194,6 +194,9 @@ jx_status jx_batch_create(const jx_host_graph *graphs, int32_t ngraphs, jx_algo 
     auto add = [&](Plan P) { plans.push_back(fit_plan(P, b->ne, max_deg)); };
     Plan Q = base;
     Q.hub_beside = !base.hub_beside;
+    add(Q);
+    Q = base;
+    Q.relabel = !base.relabel;
     add(Q);
     Q = base;
     Q.persistent = true;

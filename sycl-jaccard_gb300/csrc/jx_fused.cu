@@ -72,6 +72,7 @@ enum {
   kCtrB1,                      // work counter, B1 rows (persistent kernel)
   kCtrB0,                      // work counter, B0 rows (persistent kernel)
   kHubUnitSize,                // tasks per hub work unit of this call
+  kCtrIsolated,                // vertices without neighbours placed after the plan's rows (relabel)
   kCounters = 2 * kKeys + 32
 };
 
@@ -572,6 +573,15 @@ __device__ __forceinline__ void write_task(float I, int32_t du, int32_t dv, floa
 // ---------------------------------------------------------------- plan: degree-sorted rows
 // Degree bins of one call (a plan's choice, at most the limits of the header comment) and the
 // hub kernel's work split.
+// Where each vertex's list lies in col: [start(v), end(v)).  For a call on the graph's own ids
+// these are the CSR offsets (start = row_ptr, end = row_ptr + 1); for a call on relabelled ids
+// (see relabel in run_fused) they are arrays by new id, the lists staying where they are.
+struct Rows {
+  const int32_t *start, *end;
+  __device__ __forceinline__ int32_t s(int32_t v) const { return __ldg(start + v); }
+  __device__ __forceinline__ int32_t e(int32_t v) const { return __ldg(end + v); }
+};
+
 struct Bins {
   int32_t b0_max, b1_max, b2_max; // lane rows d <= b0_max, warp rows <= b1_max, CTA rows <= b2_max
   int32_t hub_unit;               // tasks per hub work unit at most (hub_units_kernel may use fewer)
@@ -586,14 +596,14 @@ __device__ __forceinline__ int plan_key(int32_t d, const Bins &b) {
 }
 
 template <bool kScatter>
-__global__ void plan_kernel(int32_t n, const int32_t *__restrict__ row_ptr, int32_t *__restrict__ cnt,
-                            int32_t *__restrict__ rows, Bins bins) {
+__global__ void plan_kernel(int32_t n, Rows rp, int32_t *__restrict__ cnt, int32_t *__restrict__ rows,
+                            Bins bins) {
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t u = base + threadIdx.x;
     int key = -1;
     if (u < n) {
-      const int32_t d = __ldg(row_ptr + u + 1) - __ldg(row_ptr + u);
+      const int32_t d = rp.e((int32_t)u) - rp.s((int32_t)u);
       if (d > 0) key = plan_key(d, bins);
     }
     const unsigned peers = __match_any_sync(kFull, key);
@@ -631,13 +641,12 @@ __global__ void plan_offsets_kernel(int32_t *__restrict__ cnt) {
 // against 2.8 ms with 15 clusters of 8.  R-MAT 24 (21.0M hub tasks) keeps units of 65536.
 constexpr int32_t kHubUnitsPerCluster = 4;
 constexpr int32_t kHubUnitMin = 4096;
-__global__ void hub_units_kernel(const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ rows,
-                                 int32_t *__restrict__ cnt, int32_t *__restrict__ unit_off, int32_t hub_unit,
-                                 int32_t clusters) {
+__global__ void hub_units_kernel(Rows rp, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
+                                 int32_t *__restrict__ unit_off, int32_t hub_unit, int32_t clusters) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int32_t h0 = cnt[kOffKeys + 0], h1 = cnt[kOffKeys + 32];
   int64_t tasks = 0;
-  for (int32_t i = h0; i < h1; ++i) tasks += row_ptr[rows[i] + 1] - row_ptr[rows[i]];
+  for (int32_t i = h0; i < h1; ++i) tasks += rp.e(rows[i]) - rp.s(rows[i]);
   const int64_t want = (int64_t)kHubUnitsPerCluster * (clusters > 0 ? clusters : 1);
   const int64_t fit = (tasks + want - 1) / want;
   const int64_t floor_unit = hub_unit < kHubUnitMin ? hub_unit : kHubUnitMin;
@@ -647,7 +656,7 @@ __global__ void hub_units_kernel(const int32_t *__restrict__ row_ptr, const int3
   for (int32_t i = h0; i < h1; ++i) {
     unit_off[i - h0] = run;
     const int32_t u = rows[i];
-    const int32_t d = row_ptr[u + 1] - row_ptr[u];
+    const int32_t d = rp.e(u) - rp.s(u);
     run += (d + unit - 1) / unit;
   }
   unit_off[h1 - h0] = run;
@@ -663,6 +672,59 @@ __global__ void fill_bits_kernel(int64_t n, uint32_t *__restrict__ x, uint32_t b
   for (int64_t i = (n4 << 2) + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     x[i] = bits;
+}
+
+// ---------------------------------------------------------------- relabelling
+// A call can run on relabelled vertex ids (schedule field `relabel`): new id i = position of
+// the vertex in the plan's row list (hubs first, then each bin by descending log2 degree,
+// vertices without neighbours last), every list staying where it is in col with its entries
+// mapped to new ids in the same order.  Results do not change -- membership, list positions
+// and degrees are the same -- but the vertices that appear in most lists (the high-degree ones)
+// get the smallest ids, so their weights, row sums, offsets and hub-bitmap words share fewer
+// cache lines whatever the input's numbering.  Measured on R-MAT 24 weighted: 689 ms against
+// 744 ms when the input's ids are a random bijection, but 660 against 615 ms on R-MAT's own ids,
+// which already put high degrees first and keep neighbours' ids close; the plan's order within a
+// bucket is not the ids' order, and the lists stay where they are.  Off by default.
+
+// Vertices without neighbours, after the plan's R rows: rows[R .. n).
+__global__ void relabel_isolated_kernel(int32_t n, const int32_t *__restrict__ row_ptr, int32_t *__restrict__ cnt,
+                                        int32_t *__restrict__ rows) {
+  const int lane = threadIdx.x & 31;
+  const int32_t R = cnt[kOffKeys + kKeys];
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t u = base + threadIdx.x;
+    const bool iso = u < n && __ldg(row_ptr + u + 1) == __ldg(row_ptr + u);
+    const unsigned m = __ballot_sync(kFull, iso);
+    if (!m) continue;
+    int32_t b = 0;
+    if (lane == __ffs(m) - 1) b = atomicAdd(cnt + kCtrIsolated, __popc(m));
+    b = __shfl_sync(kFull, b, __ffs(m) - 1);
+    if (iso) rows[R + b + __popc(m & ((1u << lane) - 1u))] = (int32_t)u;
+  }
+}
+
+// perm[old] = new; the new ids' list bounds, weights and row sums.
+__global__ void relabel_build_kernel(int32_t n, const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ rows,
+                                     const float *__restrict__ w, const float *__restrict__ S,
+                                     int32_t *__restrict__ perm, int32_t *__restrict__ start2,
+                                     int32_t *__restrict__ end2, float *__restrict__ w2, float *__restrict__ S2) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t u = rows[i];
+    perm[u] = (int32_t)i;
+    start2[i] = __ldg(row_ptr + u);
+    end2[i] = __ldg(row_ptr + u + 1);
+    if (w2) {
+      w2[i] = __ldg(w + u);
+      S2[i] = __ldg(S + u);
+    }
+  }
+}
+
+// col2[k] = perm[col[k]]: every list entry as a new id, in place.
+__global__ void relabel_col_kernel(int64_t e, const int32_t *__restrict__ col, const int32_t *__restrict__ perm,
+                                   int32_t *__restrict__ col2) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < e; k += (int64_t)gridDim.x * blockDim.x)
+    col2[k] = __ldg(perm + __ldg(col + k));
 }
 
 // ---------------------------------------------------------------- row sums of long rows
@@ -735,11 +797,11 @@ __global__ void __launch_bounds__(1024) rowsum_long_kernel(const int32_t *__rest
 // Row u (du <= 32): its neighbours in a 64-slot hash set `t` (this warp's), then lane k runs the
 // task of neighbour k alone.
 template <bool kEC, bool kWeighted>
-__device__ __forceinline__ void lane_row(int32_t *t, int32_t u, const int32_t *__restrict__ row_ptr,
-                                         const int32_t *__restrict__ col, const float *__restrict__ w,
-                                         const float *__restrict__ S, float *__restrict__ out) {
+__device__ __forceinline__ void lane_row(int32_t *t, int32_t u, Rows rp, const int32_t *__restrict__ col,
+                                         const float *__restrict__ w, const float *__restrict__ S,
+                                         float *__restrict__ out) {
   const int lane = threadIdx.x & 31;
-  const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
+  const int32_t us = rp.s(u), du = rp.e(u) - us;
   const uint32_t size = 2u * kB0Max;
   t[lane] = kEmpty;
   t[lane + 32] = kEmpty;
@@ -749,7 +811,7 @@ __device__ __forceinline__ void lane_row(int32_t *t, int32_t u, const int32_t *_
   if (lane < du) {
     const HashProbe probe{t, size};
     const int32_t v = __ldg(col + us + lane);
-    const int32_t vs = __ldg(row_ptr + v), dv = __ldg(row_ptr + v + 1) - vs;
+    const int32_t vs = rp.s(v), dv = rp.e(v) - vs;
     if (dv <= du) {
       int32_t mirror = -1;
       float I;
@@ -781,14 +843,14 @@ __device__ __forceinline__ void lane_row(int32_t *t, int32_t u, const int32_t *_
 
 template <bool kEC, bool kWeighted>
 __global__ void __launch_bounds__(kRowThreads) b0_kernel(
-    const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
+    Rows rp, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, const int32_t *__restrict__ cnt,
     float *__restrict__ out) {
   __shared__ int32_t tables[kRowThreads / 32][kB0Slots];
   const int32_t r0 = cnt[kOffKeys + 96], r1 = cnt[kOffKeys + 128];
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t i = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < r1; i += nwarps)
-    lane_row<kEC, kWeighted>(tables[threadIdx.x >> 5], rows[i], row_ptr, col, w, S, out);
+    lane_row<kEC, kWeighted>(tables[threadIdx.x >> 5], rows[i], rp, col, w, S, out);
 }
 
 // ---------------------------------------------------------------- task batches
@@ -803,8 +865,7 @@ __global__ void __launch_bounds__(kRowThreads) b0_kernel(
 // list to L2 when the batch is fetched: R-MAT 24 unchanged (615 / 616 / 617 against 615 ms),
 // the batch pass 1-2 % shorter; not kept.)
 template <bool kEC, bool kWeighted, class Probe, class Streams>
-__device__ __forceinline__ void run_batch(const Probe &probe, const Streams &cls,
-                                          const int32_t *__restrict__ row_ptr,
+__device__ __forceinline__ void run_batch(const Probe &probe, const Streams &cls, Rows rp,
                                           const int32_t *__restrict__ col, const float *__restrict__ w,
                                           const float *__restrict__ S, int32_t u, int32_t us, int32_t du,
                                           float Su, int32_t k0, int32_t k_end, float *__restrict__ out) {
@@ -813,8 +874,8 @@ __device__ __forceinline__ void run_batch(const Probe &probe, const Streams &cls
   float Sv = 0.0f; // weighted: S[v], loaded with the degrees rather than after each task
   if (k0 + lane < k_end) {
     v = __ldg(col + us + k0 + lane);
-    vs = __ldg(row_ptr + v);
-    dv = __ldg(row_ptr + v + 1) - vs;
+    vs = rp.s(v);
+    dv = rp.e(v) - vs;
     if (kWeighted) Sv = __ldg(S + v);
   }
   unsigned todo = __ballot_sync(kFull, v >= 0 && dv <= du);
@@ -855,12 +916,12 @@ template <bool kWeighted> __host__ __device__ constexpr int b1_warp_words() {
 
 // Row u (du <= kB1Max) by one warp: cuckoo hash of N(u) in the warp's area `t`, then its tasks.
 template <bool kEC, bool kWeighted>
-__device__ __forceinline__ void warp_row(int32_t *t, int32_t u, const int32_t *__restrict__ row_ptr,
+__device__ __forceinline__ void warp_row(int32_t *t, int32_t u, Rows rp,
                                          const int32_t *__restrict__ col, const float *__restrict__ w,
                                          const float *__restrict__ S, float *__restrict__ out) {
   const int lane = threadIdx.x & 31;
   const SmemClassStreams cls{t + kB1Slots, kB1Cap};
-  const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
+  const int32_t us = rp.s(u), du = rp.e(u) - us;
   const float Su = kWeighted ? __ldg(S + u) : 0.0f;
   const uint32_t slots = cuckoo_slots(du, kB1Slots);
   int seed = 0;
@@ -877,7 +938,7 @@ __device__ __forceinline__ void warp_row(int32_t *t, int32_t u, const int32_t *_
   if (seed < kCuckooSeeds) {
     const CuckooProbe probe = cuckoo_params(t, slots, seed);
     for (int32_t k0 = 0; k0 < du; k0 += 32)
-      run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, du, out);
+      run_batch<kEC, kWeighted>(probe, cls, rp, col, w, S, u, us, du, Su, k0, du, out);
   } else { // eviction cycles with every multiplier: linear probing (load <= 0.4)
     for (uint32_t k = lane; k < slots; k += 32) t[k] = kEmpty;
     __syncwarp();
@@ -885,14 +946,14 @@ __device__ __forceinline__ void warp_row(int32_t *t, int32_t u, const int32_t *_
     __syncwarp();
     const HashProbe probe{t, slots};
     for (int32_t k0 = 0; k0 < du; k0 += 32)
-      run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, du, out);
+      run_batch<kEC, kWeighted>(probe, cls, rp, col, w, S, u, us, du, Su, k0, du, out);
   }
   __syncwarp();
 }
 
 template <bool kEC, bool kWeighted>
 __global__ void __launch_bounds__(kRowThreads, 4) b1_kernel(
-    const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
+    Rows rp, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, const int32_t *__restrict__ cnt,
     float *__restrict__ out) {
   extern __shared__ int32_t b1_smem[];
@@ -900,13 +961,13 @@ __global__ void __launch_bounds__(kRowThreads, 4) b1_kernel(
   const int32_t r0 = cnt[kOffKeys + 64], r1 = cnt[kOffKeys + 96];
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   for (int64_t i = r0 + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); i < r1; i += nwarps)
-    warp_row<kEC, kWeighted>(t, rows[i], row_ptr, col, w, S, out);
+    warp_row<kEC, kWeighted>(t, rows[i], rp, col, w, S, out);
 }
 
 // ---------------------------------------------------------------- B2: CTA per row
 template <bool kEC, bool kWeighted, class Probe, class CS>
-__device__ __forceinline__ void b2_tasks(const Probe &probe, const CS &cls, int32_t *s_task,
-                                         const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col,
+__device__ __forceinline__ void b2_tasks(const Probe &probe, const CS &cls, int32_t *s_task, Rows rp,
+                                         const int32_t *__restrict__ col,
                                          const float *__restrict__ w, const float *__restrict__ S, int32_t u,
                                          int32_t us, int32_t du, float *__restrict__ out) {
   const int lane = threadIdx.x & 31;
@@ -920,7 +981,7 @@ __device__ __forceinline__ void b2_tasks(const Probe &probe, const CS &cls, int3
     k0 = __shfl_sync(kFull, k0, 0);
     g = __shfl_sync(kFull, g, 0);
     if (k0 >= du) break;
-    run_batch<kEC, kWeighted>(probe, cls, row_ptr, col, w, S, u, us, du, Su, k0, min(du, k0 + g), out);
+    run_batch<kEC, kWeighted>(probe, cls, rp, col, w, S, u, us, du, Su, k0, min(du, k0 + g), out);
   }
 }
 
@@ -930,8 +991,7 @@ __device__ __forceinline__ void b2_tasks(const Probe &probe, const CS &cls, int3
 // `cap` entries) start at scratch + (blockIdx.x * 32 + wid) * 8 * cap.
 template <bool kEC, bool kWeighted, bool kExact>
 __device__ __forceinline__ void cta_rows_phase(int32_t *table, int32_t *s_row, int32_t *s_task, int32_t *s_fail,
-                                               const int32_t *__restrict__ row_ptr,
-                                               const int32_t *__restrict__ col, const float *__restrict__ w,
+                                               Rows rp, const int32_t *__restrict__ col, const float *__restrict__ w,
                                                const float *__restrict__ S, const int32_t *__restrict__ rows,
                                                int32_t *__restrict__ cnt, float *__restrict__ out,
                                                int32_t *__restrict__ scratch, int cap) {
@@ -948,7 +1008,7 @@ __device__ __forceinline__ void cta_rows_phase(int32_t *table, int32_t *s_row, i
     const int32_t i = *(volatile int32_t *)s_row;
     if (i >= r1) break;
     const int32_t u = rows[i];
-    const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
+    const int32_t us = rp.s(u), du = rp.e(u) - us;
     const uint32_t slots = cuckoo_slots(du, kB2Slots);
     int seed = 0;
     for (; seed < kCuckooSeeds; ++seed) {
@@ -984,19 +1044,19 @@ __device__ __forceinline__ void cta_rows_phase(int32_t *table, int32_t *s_row, i
       if constexpr (kWeighted) {
         if (wtab) {
           const CuckooWProbe probe{cuckoo_params(table, slots, seed), reinterpret_cast<const float *>(table + slots)};
-          b2_tasks<kEC, kWeighted>(probe, rcls, s_task, row_ptr, col, w, S, u, us, du, out);
+          b2_tasks<kEC, kWeighted>(probe, rcls, s_task, rp, col, w, S, u, us, du, out);
         } else {
-          b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), rcls, s_task, row_ptr, col, w, S, u, us, du, out);
+          b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), rcls, s_task, rp, col, w, S, u, us, du, out);
         }
       } else {
-        b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), rcls, s_task, row_ptr, col, w, S, u, us, du, out);
+        b2_tasks<kEC, kWeighted>(cuckoo_params(table, slots, seed), rcls, s_task, rp, col, w, S, u, us, du, out);
       }
     } else { // eviction cycles with every multiplier: linear probing (load <= 0.43)
       for (uint32_t k = threadIdx.x; k < slots; k += blockDim.x) table[k] = kEmpty;
       __syncthreads();
       for (int32_t k = threadIdx.x; k < du; k += blockDim.x) hset_insert(table, slots, __ldg(col + us + k));
       __syncthreads();
-      b2_tasks<kEC, kWeighted>(HashProbe{table, slots}, rcls, s_task, row_ptr, col, w, S, u, us, du, out);
+      b2_tasks<kEC, kWeighted>(HashProbe{table, slots}, rcls, s_task, rp, col, w, S, u, us, du, out);
     }
     __syncthreads();
   }
@@ -1004,12 +1064,12 @@ __device__ __forceinline__ void cta_rows_phase(int32_t *table, int32_t *s_row, i
 
 template <bool kEC, bool kWeighted, bool kExact>
 __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
-    const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
+    Rows rp, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
     float *__restrict__ out, int32_t *__restrict__ scratch, int cap) {
   extern __shared__ int32_t table[];
   __shared__ int32_t s_row, s_task, s_fail;
-  cta_rows_phase<kEC, kWeighted, kExact>(table, &s_row, &s_task, &s_fail, row_ptr, col, w, S, rows, cnt, out,
+  cta_rows_phase<kEC, kWeighted, kExact>(table, &s_row, &s_task, &s_fail, rp, col, w, S, rows, cnt, out,
                                          scratch, cap);
 }
 
@@ -1020,7 +1080,7 @@ __global__ void __launch_bounds__(kB2Threads, 1) b2_kernel(
 // phases; the unit index and task counter live in rank 0's shared memory.
 template <bool kEC, bool kWeighted, int kCl>
 __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
-    const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
+    Rows rp, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
     const int32_t *__restrict__ unit_off, uint32_t *__restrict__ bitmaps, int64_t words,
     float *__restrict__ out, int32_t *__restrict__ scratch, int cap, Bins bins) {
@@ -1056,7 +1116,7 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
       if (unit_off[mid] <= unit) lo = mid; else hi = mid - 1;
     }
     const int32_t u = rows[h0 + lo];
-    const int32_t us = __ldg(row_ptr + u), du = __ldg(row_ptr + u + 1) - us;
+    const int32_t us = rp.s(u), du = rp.e(u) - us;
     const int32_t k_begin = (unit - unit_off[lo]) * unit_size;
     const int32_t k_end = min(du, k_begin + unit_size);
     if constexpr (kWords != 0) {
@@ -1085,10 +1145,10 @@ __global__ void __launch_bounds__(kHubThreads, 1) hub_kernel(
       g = __shfl_sync(kFull, g, 0);
       if (k0 >= k_end) break;
       if constexpr (kWords != 0)
-        run_batch<kEC, kWeighted>(FilterProbe{filt, bm, kWords * 32}, cls, row_ptr, col, w, S, u, us, du, Su, k0,
+        run_batch<kEC, kWeighted>(FilterProbe{filt, bm, kWords * 32}, cls, rp, col, w, S, u, us, du, Su, k0,
                                   min(k_end, k0 + g), out);
       else
-        run_batch<kEC, kWeighted>(BitmapProbe{bm}, cls, row_ptr, col, w, S, u, us, du, Su, k0, min(k_end, k0 + g),
+        run_batch<kEC, kWeighted>(BitmapProbe{bm}, cls, rp, col, w, S, u, us, du, Su, k0, min(k_end, k0 + g),
                                   out);
     }
     cluster.sync();
@@ -1117,13 +1177,13 @@ constexpr int kB0Fetch = 32; // lane rows a warp takes per fetch
 
 template <bool kEC, bool kWeighted, bool kExact>
 __global__ void __launch_bounds__(kB2Threads, 1) rows_kernel(
-    const int32_t *__restrict__ row_ptr, const int32_t *__restrict__ col, const float *__restrict__ w,
+    Rows rp, const int32_t *__restrict__ col, const float *__restrict__ w,
     const float *__restrict__ S, const int32_t *__restrict__ rows, int32_t *__restrict__ cnt,
     float *__restrict__ out, int32_t *__restrict__ scratch, int cap_b2) {
   extern __shared__ int32_t area[];
   __shared__ int32_t s_row, s_task, s_fail;
   static_assert((kB2Threads / 32) * b1_warp_words<kWeighted>() <= kB2Slots, "warp-row tables");
-  cta_rows_phase<kEC, kWeighted, kExact>(area, &s_row, &s_task, &s_fail, row_ptr, col, w, S, rows, cnt, out, scratch,
+  cta_rows_phase<kEC, kWeighted, kExact>(area, &s_row, &s_task, &s_fail, rp, col, w, S, rows, cnt, out, scratch,
                                          cap_b2);
   // warp rows, then lane rows: each warp in its own part of the area (no barrier between them;
   // every thread left the CTA-row phase together)
@@ -1136,7 +1196,7 @@ __global__ void __launch_bounds__(kB2Threads, 1) rows_kernel(
       if (lane == 0) i = r0 + atomicAdd(cnt + kCtrB1, kB1Fetch);
       i = __shfl_sync(kFull, i, 0);
       if (i >= r1) break;
-      for (int32_t j = i; j < min(r1, i + kB1Fetch); ++j) warp_row<kEC, kWeighted>(t, rows[j], row_ptr, col, w, S, out);
+      for (int32_t j = i; j < min(r1, i + kB1Fetch); ++j) warp_row<kEC, kWeighted>(t, rows[j], rp, col, w, S, out);
     }
   }
   {
@@ -1146,7 +1206,7 @@ __global__ void __launch_bounds__(kB2Threads, 1) rows_kernel(
       if (lane == 0) i = r0 + atomicAdd(cnt + kCtrB0, kB0Fetch);
       i = __shfl_sync(kFull, i, 0);
       if (i >= r1) break;
-      for (int32_t j = i; j < min(r1, i + kB0Fetch); ++j) lane_row<kEC, kWeighted>(t, rows[j], row_ptr, col, w, S, out);
+      for (int32_t j = i; j < min(r1, i + kB0Fetch); ++j) lane_row<kEC, kWeighted>(t, rows[j], rp, col, w, S, out);
     }
   }
 }
@@ -1326,6 +1386,7 @@ Plan apply_schedule(Plan P, const jx_schedule *sch, int64_t e, int64_t max_degre
     if (sch->hub_unit > 0) P.hub_unit = sch->hub_unit;
     if (sch->hub_batch > 0) P.hub_batch = sch->hub_batch;
     if (sch->hub_beside) P.hub_beside = sch->hub_beside > 0;
+    if (sch->relabel) P.relabel = sch->relabel > 0;
     if (sch->hub_cluster == 4 || sch->hub_cluster == 8) {
       P.hub_cluster = sch->hub_cluster;
       P.hub_clusters = resident_hub_clusters(P.hub_cluster);
@@ -1338,6 +1399,7 @@ static Bins bins_of(const Plan &P) { return Bins{P.b0_max, P.b1_max, P.b2_max, P
 
 struct Layout {
   size_t cnt, rows, unit_off, S, scratch, bitmaps, total;
+  size_t perm, start2, end2, w2, S2, col2; // relabelled ids (P.relabel)
   size_t hub_scratch; // byte offset of the hub kernel's class streams inside the scratch region
   int64_t words;
 };
@@ -1360,6 +1422,15 @@ static Layout layout(int32_t n, int32_t e, bool weighted_vc, const Plan &P) {
   L.scratch = off;
   off += weighted_vc ? align256(sizeof(int32_t) * (P.hub_beside ? b2_ids + hub_ids : std::max(b2_ids, hub_ids))) : 0;
   L.bitmaps = off;  off += align256(sizeof(uint32_t) * (size_t)L.words * P.hub_clusters);
+  L.perm = L.start2 = L.end2 = L.w2 = L.S2 = L.col2 = 0;
+  if (P.relabel) {
+    L.perm = off;   off += align256(sizeof(int32_t) * (size_t)n);
+    L.start2 = off; off += align256(sizeof(int32_t) * (size_t)n);
+    L.end2 = off;   off += align256(sizeof(int32_t) * (size_t)n);
+    L.w2 = off;     off += weighted_vc ? align256(sizeof(float) * (size_t)n) : 0;
+    L.S2 = off;     off += weighted_vc ? align256(sizeof(float) * (size_t)n) : 0;
+    L.col2 = off;   off += align256(sizeof(int32_t) * (size_t)e);
+  }
   L.total = off;
   return L;
 }
@@ -1426,15 +1497,17 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
   if ((ce = cudaMemsetAsync(bitmaps, 0, sizeof(uint32_t) * (size_t)L.words * P.hub_clusters, s)) != cudaSuccess)
     return set_cuda_error(ce);
   const Bins bins = bins_of(P);
-  plan_kernel<false><<<sms * 4, 256, 0, s>>>(n, g.row_ptr, cnt, rows, bins);
-  if ((st = check_launch()) != JX_OK) return st;
-  plan_offsets_kernel<<<1, kKeys, 0, s>>>(cnt);
-  if ((st = check_launch()) != JX_OK) return st;
-  plan_kernel<true><<<sms * 4, 256, 0, s>>>(n, g.row_ptr, cnt, rows, bins);
-  if ((st = check_launch()) != JX_OK) return st;
-  hub_units_kernel<<<1, 32, 0, s>>>(g.row_ptr, rows, cnt, unit_off, bins.hub_unit, P.hub_clusters);
-  if ((st = check_launch()) != JX_OK) return st;
-  prof_mark("plan", s);
+  const Rows orig{g.row_ptr, g.row_ptr + 1};
+  auto plan = [&](Rows rp) -> jx_status {
+    plan_kernel<false><<<sms * 4, 256, 0, s>>>(n, rp, cnt, rows, bins);
+    jx_status r = check_launch();
+    if (r != JX_OK) return r;
+    plan_offsets_kernel<<<1, kKeys, 0, s>>>(cnt);
+    if ((r = check_launch()) != JX_OK) return r;
+    plan_kernel<true><<<sms * 4, 256, 0, s>>>(n, rp, cnt, rows, bins);
+    return check_launch();
+  };
+  if ((st = plan(orig)) != JX_OK) return st;
   if (kWeighted && !row_sums) {
     // rows of the warp and lane bins, then the longer ones from the plan's row lists
     if ((st = rowsum_upto(n, g.row_ptr, g.col_idx, w, S_ws, P.b1_max, s)) != JX_OK) return st;
@@ -1442,6 +1515,35 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
     if ((st = check_launch()) != JX_OK) return st;
     prof_mark("rowsum", s);
   }
+  // the arrays the row kernels work on: the graph's own, or relabelled (ids by plan position)
+  Rows rp = orig;
+  const int32_t *colA = g.col_idx;
+  const float *wA = w, *SA = S;
+  if (P.relabel) {
+    int32_t *perm = reinterpret_cast<int32_t *>(ws + L.perm);
+    int32_t *start2 = reinterpret_cast<int32_t *>(ws + L.start2);
+    int32_t *end2 = reinterpret_cast<int32_t *>(ws + L.end2);
+    float *w2 = kWeighted ? reinterpret_cast<float *>(ws + L.w2) : nullptr;
+    float *S2 = kWeighted ? reinterpret_cast<float *>(ws + L.S2) : nullptr;
+    int32_t *col2 = reinterpret_cast<int32_t *>(ws + L.col2);
+    relabel_isolated_kernel<<<sms * 4, 256, 0, s>>>(n, g.row_ptr, cnt, rows);
+    if ((st = check_launch()) != JX_OK) return st;
+    relabel_build_kernel<<<sms * 4, 256, 0, s>>>(n, g.row_ptr, rows, w, S, perm, start2, end2, w2, S2);
+    if ((st = check_launch()) != JX_OK) return st;
+    relabel_col_kernel<<<sms * 8, 256, 0, s>>>(g.e, g.col_idx, perm, col2);
+    if ((st = check_launch()) != JX_OK) return st;
+    prof_mark("relabel", s);
+    rp = Rows{start2, end2};
+    colA = col2;
+    wA = w2;
+    SA = S2;
+    // the plan again, on the new ids (the same rows in the same bins, now numbered in order)
+    if ((ce = cudaMemsetAsync(cnt, 0, sizeof(int32_t) * kCounters, s)) != cudaSuccess) return set_cuda_error(ce);
+    if ((st = plan(rp)) != JX_OK) return st;
+  }
+  hub_units_kernel<<<1, 32, 0, s>>>(rp, rows, cnt, unit_off, bins.hub_unit, P.hub_clusters);
+  if ((st = check_launch()) != JX_OK) return st;
+  prof_mark("plan", s);
   fill_bits_kernel<<<sms * 4, 256, 0, s>>>(g.e, reinterpret_cast<uint32_t *>(out), kUnwritten);
   if ((st = check_launch()) != JX_OK) return st;
   prof_mark("sentinel_fill", s);
@@ -1475,8 +1577,7 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
     cfg.attrs = cluster_attr;
     cfg.numAttrs = 1;
     int32_t *hub_scratch = scratch ? scratch + L.hub_scratch / sizeof(int32_t) : nullptr;
-    ce = cudaLaunchKernelEx(&cfg, hub, (const int32_t *)g.row_ptr,
-                            (const int32_t *)g.col_idx, w, (const float *)S, (const int32_t *)rows, cnt,
+    ce = cudaLaunchKernelEx(&cfg, hub, rp, colA, wA, SA, (const int32_t *)rows, cnt,
                             (const int32_t *)unit_off, bitmaps, (int64_t)L.words, out, hub_scratch, P.cap_hub, bins);
     if (ce != cudaSuccess) return set_cuda_error(ce);
     if ((st = check_launch()) != JX_OK) return st;
@@ -1488,30 +1589,30 @@ static jx_status run_fused(const jx_csr &g, const float *w, float *out, char *ws
     auto kern = (kWeighted && P.b2_exact) ? rows_kernel<kEC, kWeighted, true> : rows_kernel<kEC, kWeighted, false>;
     ce = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b2);
     if (ce != cudaSuccess) return set_cuda_error(ce);
-    kern<<<P.b2_ctas, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out, scratch, P.cap_b2);
+    kern<<<P.b2_ctas, kB2Threads, smem_b2, s>>>(rp, colA, wA, SA, rows, cnt, out, scratch, P.cap_b2);
     if ((st = check_launch()) != JX_OK) return st;
     prof_mark("row_bins", s);
   } else {
     auto b2 = (kWeighted && P.b2_exact) ? b2_kernel<kEC, kWeighted, true> : b2_kernel<kEC, kWeighted, false>;
     ce = cudaFuncSetAttribute(b2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b2);
     if (ce != cudaSuccess) return set_cuda_error(ce);
-    b2<<<P.b2_ctas, kB2Threads, smem_b2, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out, scratch, P.cap_b2);
+    b2<<<P.b2_ctas, kB2Threads, smem_b2, s>>>(rp, colA, wA, SA, rows, cnt, out, scratch, P.cap_b2);
     if ((st = check_launch()) != JX_OK) return st;
     prof_mark("cta_rows", s);
     const size_t smem_b1 = sizeof(int32_t) * (kRowThreads / 32) * b1_warp_words<kWeighted>();
     ce = cudaFuncSetAttribute(b1_kernel<kEC, kWeighted>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_b1);
     if (ce != cudaSuccess) return set_cuda_error(ce);
     int b1_grid = P.b1_ctas;
-    if (b1_grid <= 0) { // every CTA that fits at once: 4 per SM unweighted, 3 weighted (shared memory)
+    if (b1_grid <= 0) { // every CTA that fits at once (registers and shared memory: 4 per SM on GB300)
       int per_sm = 0;
       ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, b1_kernel<kEC, kWeighted>, kRowThreads, smem_b1);
       if (ce != cudaSuccess) return set_cuda_error(ce);
       b1_grid = std::max(1, per_sm) * sms;
     }
-    b1_kernel<kEC, kWeighted><<<b1_grid, kRowThreads, smem_b1, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
+    b1_kernel<kEC, kWeighted><<<b1_grid, kRowThreads, smem_b1, s>>>(rp, colA, wA, SA, rows, cnt, out);
     if ((st = check_launch()) != JX_OK) return st;
     prof_mark("warp_rows", s);
-    b0_kernel<kEC, kWeighted><<<P.b0_ctas, kRowThreads, 0, s>>>(g.row_ptr, g.col_idx, w, S, rows, cnt, out);
+    b0_kernel<kEC, kWeighted><<<P.b0_ctas, kRowThreads, 0, s>>>(rp, colA, wA, SA, rows, cnt, out);
     if ((st = check_launch()) != JX_OK) return st;
     prof_mark("lane_rows", s);
   }
@@ -1571,6 +1672,7 @@ static Plan noalloc_plan() {
   const int sms = sm_count();
   Plan P{8, 1, 1024, 1024, sms * 3, sms * 8};
   P.hub_beside = false; // one stream: no second stream or events to create
+  P.relabel = false;    // no room for a relabelled copy of the lists
   return P;
 }
 

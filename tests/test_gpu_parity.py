@@ -271,6 +271,8 @@ SCHEDULES = [
     {"persistent": 0, "hub_beside": -1, "lane_max": 8, "warp_max": 64, "cta_max": 1024, "hub_unit": 300,
      "hub_batch": 1},
     {"persistent": 1, "hub_beside": 1, "hub_cluster": 4, "lane_max": 1, "warp_max": 1, "cta_max": 1},  # all hub rows
+    {"relabel": 1},  # vertex ids renumbered by degree
+    {"relabel": 1, "persistent": 1, "hub_cluster": 8, "cta_max": 4096, "hub_unit": 1000},
 ]
 
 
@@ -278,8 +280,9 @@ SCHEDULES = [
 @pytest.mark.parametrize("mode", ["ec", "vc", "vcw"])
 def test_schedules_match_oracle(jx, O, sch, mode):
     """Every launch schedule -- the persistent row kernel, the hub kernel beside or before the
-    rows, and bin limits that move rows between the lane, warp, CTA and hub paths -- gives the
-    oracle's results bit for bit, on a skewed graph and on one with repeated neighbours."""
+    rows, bin limits that move rows between the lane, warp, CTA and hub paths, and vertex ids
+    renumbered by degree -- gives the oracle's results bit for bit, on a skewed graph and on one
+    with repeated neighbours."""
     import torch
     rng = np.random.default_rng(5)
     graphs = [jx.graphgen.rmat(14, 16, 0.57, 0.19, 0.19, seed=77)]
