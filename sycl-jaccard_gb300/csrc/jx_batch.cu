@@ -186,8 +186,8 @@ jx_status jx_batch_create(const jx_host_graph *graphs, int32_t ngraphs, jx_algo 
 
   // candidate plans (the default first); the autotuner keeps the fastest on this batch: one
   // kernel per bin against the persistent row launch, the hub kernel beside or before the rows,
-  // bin limits (which rows take the lane, warp, CTA or hub path), the hub fetch cap, and the
-  // grids of the lane and warp kernels
+  // the graph's own vertex ids or relabelled ones, bin limits (which rows take the lane, warp,
+  // CTA or hub path), the hub fetch cap, and the grids of the lane and warp kernels
   const Plan base = fit_plan(default_plan(), b->ne, max_deg);
   std::vector<Plan> plans{base};
   if (tune) {
